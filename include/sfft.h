@@ -1,0 +1,194 @@
+/*
+ * sfft.h — GB300 sparse FFT engine, drop-in C interface of sFFT 0.1.
+ *
+ * The first block keeps the reference's types and six exported functions
+ * (sFFT 0.1 src/sfft.h:34-50 and :158-167) with the same names, layouts,
+ * argument meanings and ownership rules; a program or binding written for
+ * libsfft.so of sFFT 0.1 links against this library unchanged.  The second
+ * block adds entry points for device-resident, batched, sparse and
+ * reduced-precision use.  All entry points are extern "C", take plain
+ * pointers and sizes, and never abort: failures return NULL / a negative
+ * status and leave a message for sfft_last_error().
+ */
+#ifndef SFFT_GB300_SFFT_H
+#define SFFT_GB300_SFFT_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+#include <unordered_map>
+#endif
+
+/* complex_t: C99 double complex, as sFFT 0.1 src/fft.h:42-45 (g++ accepts
+ * the _Complex keyword as an extension, as the reference relies on). */
+#ifndef SFFT_COMPLEX_T_DEFINED
+#define SFFT_COMPLEX_T_DEFINED
+typedef double _Complex complex_t;
+#endif
+
+/* FFTW planner flags accepted (and, as in the reference, not needed) by
+ * sfft_make_plan; values of fftw3.h, which the reference binding hard-codes
+ * (python/sfft/sfft.py:7-8). */
+#ifndef FFTW_ESTIMATE
+#define FFTW_MEASURE (0U)
+#define FFTW_ESTIMATE (1U << 6)
+#endif
+
+#ifdef __cplusplus
+/* sFFT 0.1 src/sfft.h:34-35 (the reference used std::tr1::unordered_map). */
+typedef std::unordered_map<int, complex_t> sfft_output;
+#endif
+
+/* sFFT 0.1 src/sfft.h:37-42 */
+enum sfft_version
+{
+  SFFT_VERSION_1,
+  SFFT_VERSION_2,
+  SFFT_VERSION_3
+};
+
+/* sFFT 0.1 src/sfft.h:44-50.  `data` is opaque here (device-resident plan). */
+struct sfft_plan
+{
+  enum sfft_version version;
+  unsigned int n;
+  unsigned int k;
+  void *data;
+};
+typedef struct sfft_plan sfft_plan;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- the reference's API (sFFT 0.1 src/sfft.h:158-167) ------------------ */
+
+/* src/sfft.cc:60-63.  16-byte aligned; here page-locked host memory, so
+ * transfers to the GPU run at full link speed.  Free with sfft_free. */
+void *sfft_malloc(size_t s);
+/* src/sfft.cc:65-69 */
+void sfft_free(void *p);
+
+/* src/sfft.cc:71-101.  n must be a power of two (the reference floors n
+ * inside the plan but not in sfft_exec).  Returns NULL for an unknown
+ * version, for (n, k) outside the algorithm's domain (v1/v2: every bucket
+ * count >= 2k+1; v3: k >= 8) or when no CUDA device is usable. */
+sfft_plan *sfft_make_plan(int n, int k, enum sfft_version version, int fftw_optimization);
+/* src/sfft.cc:103-117 (frees everything, including the plan itself). */
+void sfft_free_plan(sfft_plan *plan);
+/* src/sfft.cc:119-137.  in: n complex values; out: n complex values, fully
+ * overwritten (zeros except the recovered coefficients).  Either may be a
+ * host or a device pointer.  v1/v2 values are those of the reference, i.e.
+ * the complex conjugates of the spectrum (src/computefourier-1.0-2.0.cc:
+ * 383-398).  Randomness: glibc random()/drand48(), drawn in the reference's
+ * order. */
+void sfft_exec(sfft_plan *plan, complex_t *in, complex_t *out);
+/* src/sfft.cc:139-147.  `num` transforms with one plan, batched on the
+ * GPU; draws happen in signal order. */
+void sfft_exec_many(sfft_plan *plan, int num, complex_t **in, complex_t **out);
+
+/* ---- additions (no counterpart in the reference) ------------------------ */
+
+enum sfft_precision
+{
+  SFFT_PREC_FP64 = 0,           /* parity form: bit-exact v1/v2 */
+  SFFT_PREC_FP32 = 1            /* fold, bucket FFTs, estimation in FP32 */
+};
+
+enum sfft_input_type
+{
+  SFFT_IN_C128 = 0,             /* complex128 (complex_t) */
+  SFFT_IN_C64 = 1               /* complex64 (float pairs) */
+};
+
+struct sfft_options
+{
+  int precision;                /* enum sfft_precision */
+  int device;                   /* CUDA device ordinal, -1 = current */
+  int max_batch;                /* signals per launch (0 = default 16) */
+};
+typedef struct sfft_options sfft_options;
+
+/* As sfft_make_plan with options (NULL = FP64, current device). */
+sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_optimization,
+                             const sfft_options *opt);
+
+/* Message of the last failure on this thread ("" if none). */
+const char *sfft_last_error(void);
+
+/* Number of coefficients one transform can return (sizes sparse outputs). */
+long sfft_output_capacity(const sfft_plan *plan);
+
+/* One transform with a sparse result: writes up to `cap` (index, value)
+ * pairs (host or device buffers) and returns their number, or -1. */
+long sfft_exec_sparse(sfft_plan *plan, const complex_t *in, int *out_idx, complex_t *out_val,
+                      long cap);
+
+/* Batched, device-resident, asynchronous.  in: host array of `num` device
+ * pointers to signals of type `in_type`.  Outputs are device buffers:
+ * out_idx[s * out_stride + i], out_val likewise (complex128 for FP64 plans,
+ * complex64 for FP32 plans), out_count[s].  `stream` is a cudaStream_t
+ * (NULL = the plan's stream).  Returns 0 or -1. */
+int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type, int *out_idx,
+                    void *out_val, int *out_count, long out_stride, void *stream);
+
+/* Waits for the plan's work and reports device-side errors: 0 or -1. */
+int sfft_sync(sfft_plan *plan);
+
+/* Diagnostics of the last transform of batch slot 0, for parity checks.
+ * what: 0 permutations a[L] then ai[L] (int); 1 selected buckets J[L][2k]
+ * (int); 2 vote counts (n int); 3 bucket values x_samp (complex, plan
+ * precision); 4 v2 comb residues (int, count returned); 5 v3 rounds;
+ * 6 v3 estimates as (round, stage, frequency, re, im) doubles.
+ * Returns the number of elements written, or -1. */
+long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap);
+
+/* Stage timing with CUDA events recorded on the launching stream.
+ * sfft_profile(plan, 1) starts (and zeroes) it; sfft_profile_read waits for
+ * the recorded launches and writes the summed milliseconds per stage
+ * (v1/v2: 0 comb filter, 1 permuted-filter fold, 2 bucket FFT + top-k
+ * selection + voting, 3 median estimation; v3: 0 filters, 1 peeling);
+ * it returns the number of timed launches, or -1. */
+int sfft_profile(sfft_plan *plan, int enable);
+long sfft_profile_read(sfft_plan *plan, double *stage_ms, int nstage);
+/* Number of GPU kernels this library has launched in this process. */
+long sfft_kernel_launches(void);
+
+/* Host-only plan queries (no GPU needed): the parameters a plan for
+ * (n, k, version) would use, as the reference computes them.  fields:
+ * v1/v2: B_loc, B_thresh, B_est, W_Comb, Comb_loops, loops_loc,
+ * loops_thresh, loops_est, w_loc, w_est, x_samp_size; v3: W_Man, B_g1,
+ * w_g1, B_g2, w_g2.  Returns the number of fields written, or -1. */
+int sfft_describe_plan(int n, int k, enum sfft_version version, long *fields, int nfields);
+/* The filter a plan would use: which 0 = location / first Gaussian,
+ * 1 = estimation / second Gaussian; time taps (2*w doubles) and the
+ * n-point spectrum (2*n doubles, may be NULL).  Returns w, or -1. */
+int sfft_describe_filter(int n, int k, enum sfft_version version, int which, double *time, long time_cap,
+                         double *freq, long freq_cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#ifdef __cplusplus
+/* The form the sFFT documentation gives (doc/usage.rst:77): a map from
+ * frequency to coefficient, filled through sfft_exec_sparse. */
+#include <vector>
+inline int sfft_exec_output(sfft_plan *plan, const complex_t *in, sfft_output *out)
+{
+  long cap = sfft_output_capacity(plan);
+  if (cap < 0)
+    return -1;
+  std::vector<int> idx((size_t)cap);
+  std::vector<complex_t> val((size_t)cap);
+  long c = sfft_exec_sparse(plan, in, idx.data(), val.data(), cap);
+  if (c < 0)
+    return -1;
+  out->clear();
+  for (long i = 0; i < c; i++)
+    (*out)[idx[(size_t)i]] = val[(size_t)i];
+  return 0;
+}
+#endif
+
+#endif

@@ -81,6 +81,8 @@ def lib():
         L.oracle_dbg_comb.restype = ip
         L.oracle_dbg_comb.argtypes = [vp, ip]
         L.oracle_dbg_v3.argtypes = [vp, ip]
+        L.oracle_dbg_v3_trace.restype = ctypes.c_long
+        L.oracle_dbg_v3_trace.argtypes = [vp, vp, ctypes.c_long]
         L.shim_fft.argtypes = [ctypes.c_int, vp, ctypes.c_int]
         _lib = L
     return _lib
@@ -174,6 +176,11 @@ class OraclePlan:
         c = ctypes.c_int()
         ptr = self.lib.oracle_dbg_comb(self.h, ctypes.byref(c))
         return np.ctypeslib.as_array(ptr, shape=(max(c.value, 1),))[:c.value].copy()
+
+    def v3_trace(self):
+        buf = np.empty((1 << 16, 5), dtype=np.float64)
+        c = self.lib.oracle_dbg_v3_trace(self.h, buf.ctypes.data, buf.shape[0])
+        return buf[:c].copy()
 
     def v3_debug(self):
         v = (ctypes.c_int * 8)()

@@ -305,6 +305,9 @@ typedef struct
   int *est_f;
   double *est_v;
   int v3dbg[8];
+  /* v3 trace: per found tone (round, stage, key, value) */
+  double *trace;
+  long trace_n, trace_cap;
 } oscratch;
 
 struct oracle_plan
@@ -358,7 +361,23 @@ static void alloc_scratch(oracle_plan *p, oscratch *s)
       s->perm_x = (double *)calloc(2 * (size_t)(p->w_g2 + 1), sizeof(double));
       s->est_f = (int *)calloc(cap, sizeof(int));
       s->est_v = (double *)calloc(2 * (size_t)cap, sizeof(double));
+      s->trace_cap = 1 << 16;
+      s->trace = (double *)calloc(5 * (size_t)s->trace_cap, sizeof(double));
     }
+}
+
+static void trace_add(oscratch *s, int round, int stage, int key, double re, double im)
+{
+  if (s->trace_n < s->trace_cap)
+    {
+      double *t = s->trace + 5 * s->trace_n;
+      t[0] = round;
+      t[1] = stage;
+      t[2] = key;
+      t[3] = re;
+      t[4] = im;
+    }
+  s->trace_n++;
 }
 
 static void free_scratch(oscratch *s)
@@ -366,7 +385,7 @@ static void free_scratch(oscratch *s)
   void *ptrs[] = { s->a, s->ai, s->x_samp, s->x_sampt, s->samples, s->score,
     s->hits, s->J, s->Jall, s->comb, s->comb_xs, s->comb_samples,
     s->pa_first, s->pa_second, s->nth_tmp, s->man, s->gauss, s->gperm,
-    s->perm_x, s->est_f, s->est_v
+    s->perm_x, s->est_f, s->est_v, s->trace
   };
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++)
     free(ptrs[i]);
@@ -1101,10 +1120,12 @@ static void o_alternate_fft(oracle_plan *p, oscratch *s, const double *x, omap *
   dbg[6] = 0;
 
   o_mansour_filt(p, s, x, init_offset);
+  s->trace_n = 0;
   int found = 0;
   int found_now = o_estimate_freq_mansour(W, MAN, init_offset, n, EF, EV);
   for (int i = 0; i < found_now; i++)
     {
+      trace_add(s, -2, 0, EF[i], EV[2 * i], EV[2 * i + 1]);
       long q = omap_get(ans, EF[i]);
       ans->vals[2 * q] = EV[2 * i];
       ans->vals[2 * q + 1] = EV[2 * i + 1];
@@ -1130,6 +1151,7 @@ static void o_alternate_fft(oracle_plan *p, oscratch *s, const double *x, omap *
   found_now = o_estimate_freq_gauss(B1, G1, init_G_offset, n, 1, 0, jump, p->f_loc, EF, EV);
   for (int i = 0; i < found_now; i++)
     {
+      trace_add(s, -1, 1, EF[i], EV[2 * i], EV[2 * i + 1]);
       long q = omap_get(ans, EF[i]);
       double vr = ans->vals[2 * q], vi = ans->vals[2 * q + 1];
       if (vr * vr + vi * vi == 0)
@@ -1159,6 +1181,7 @@ static void o_alternate_fft(oracle_plan *p, oscratch *s, const double *x, omap *
         found_now = o_estimate_freq_gauss(B2, G2, init_G_offset, n, a, b, jump, p->f_est, EF, EV);
       for (int i = 0; i < found_now; i++)
         {
+          trace_add(s, nana, stage, EF[i], EV[2 * i], EV[2 * i + 1]);
           long q = omap_get(ans, EF[i]);
           double vr = ans->vals[2 * q], vi = ans->vals[2 * q + 1];
           if (vr * vr + vi * vi == 0)
@@ -1354,4 +1377,13 @@ const int *oracle_dbg_comb(const oracle_plan *p, int *count)
 void oracle_dbg_v3(const oracle_plan *p, int *vals)
 {
   memcpy(vals, p->scr[0].v3dbg, sizeof(int) * 8);
+}
+
+long oracle_dbg_v3_trace(const oracle_plan *p, double *out, long cap)
+{
+  long n = p->scr[0].trace_n < p->scr[0].trace_cap ? p->scr[0].trace_n : p->scr[0].trace_cap;
+  if (n > cap)
+    n = cap;
+  memcpy(out, p->scr[0].trace, sizeof(double) * 5 * (size_t)n);
+  return n;
 }

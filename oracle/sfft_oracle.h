@@ -65,6 +65,10 @@ const double *oracle_dbg_xsamp(const oracle_plan *p);        /* buckets */
 const int *oracle_dbg_comb(const oracle_plan *p, int *count);
 /* v3: a, ai, b, init_offset, init_G_offset, passes, early_exit, n_found */
 void oracle_dbg_v3(const oracle_plan *p, int *vals);
+/* v3: every tone estimate of the last exec as (round, stage, key, re, im);
+ * round -2 is the first comb pass, -1 the first Gaussian pass, then the
+ * round-robin loop.  Returns the number of records. */
+long oracle_dbg_v3_trace(const oracle_plan *p, double *out, long cap);
 
 #ifdef __cplusplus
 }

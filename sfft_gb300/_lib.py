@@ -1,0 +1,91 @@
+"""ctypes binding of libsfft.so (the C interface of include/sfft.h).
+
+There is no fallback: if the library is missing this module raises, and a
+plan cannot be made without a CUDA device.
+"""
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsfft.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "sfft.h")
+
+SFFT_VERSION_1, SFFT_VERSION_2, SFFT_VERSION_3 = 0, 1, 2
+SFFT_PREC_FP64, SFFT_PREC_FP32 = 0, 1
+SFFT_IN_C128, SFFT_IN_C64 = 0, 1
+FFTW_MEASURE = 0
+FFTW_ESTIMATE = 1 << 6
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("device", ctypes.c_int), ("max_batch", ctypes.c_int)]
+
+
+class Plan(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_int), ("n", ctypes.c_uint), ("k", ctypes.c_uint),
+                ("data", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def header_functions():
+    """Names of the functions include/sfft.h declares."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    block = src.split('extern "C" {', 1)[1].split("#ifdef __cplusplus\n}", 1)[0]
+    return sorted(set(re.findall(r"\b(sfft_\w+)\s*\(", block)))
+
+
+def load(build_if_missing=False):
+    """The loaded library (ctypes.CDLL) with argument types set."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from . import build
+            build.build()
+        else:
+            raise ImportError(f"{LIB_PATH} is not built (python -m sfft_gb300.build)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, cp, ci, cl = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_long
+    PP = ctypes.POINTER(Plan)
+    L.sfft_malloc.restype = vp
+    L.sfft_malloc.argtypes = [ctypes.c_size_t]
+    L.sfft_free.argtypes = [vp]
+    L.sfft_make_plan.restype = PP
+    L.sfft_make_plan.argtypes = [ci, ci, ci, ci]
+    L.sfft_make_plan_ex.restype = PP
+    L.sfft_make_plan_ex.argtypes = [ci, ci, ci, ci, ctypes.POINTER(Options)]
+    L.sfft_free_plan.argtypes = [PP]
+    L.sfft_exec.argtypes = [PP, vp, vp]
+    L.sfft_exec_many.argtypes = [PP, ci, vp, vp]
+    L.sfft_last_error.restype = cp
+    L.sfft_output_capacity.restype = cl
+    L.sfft_output_capacity.argtypes = [PP]
+    L.sfft_exec_sparse.restype = cl
+    L.sfft_exec_sparse.argtypes = [PP, vp, vp, vp, cl]
+    L.sfft_exec_batch.restype = ci
+    L.sfft_exec_batch.argtypes = [PP, ci, vp, ci, vp, vp, vp, cl, vp]
+    L.sfft_sync.restype = ci
+    L.sfft_sync.argtypes = [PP]
+    L.sfft_debug_fetch.restype = cl
+    L.sfft_debug_fetch.argtypes = [PP, ci, vp, cl]
+    L.sfft_describe_plan.restype = ci
+    L.sfft_describe_plan.argtypes = [ci, ci, ci, ctypes.POINTER(cl), ci]
+    L.sfft_describe_filter.restype = ci
+    L.sfft_describe_filter.argtypes = [ci, ci, ci, ci, vp, cl, vp, cl]
+    L.sfft_profile.restype = ci
+    L.sfft_profile.argtypes = [PP, ci]
+    L.sfft_profile_read.restype = cl
+    L.sfft_profile_read.argtypes = [PP, ctypes.POINTER(ctypes.c_double), ci]
+    L.sfft_kernel_launches.restype = cl
+    L.sfft_kernel_launches.argtypes = []
+    _lib = L
+    return L
+
+
+def last_error():
+    return load().sfft_last_error().decode()

@@ -1,0 +1,981 @@
+// api.cc — the C interface of include/sfft.h on top of the GB300 kernels.
+//
+// A plan owns device-resident filters, twiddle tables and a workspace for
+// `max_batch` signals.  Execution draws the reference's random numbers on
+// the host (glibc random()/drand48(), same order as src/computefourier-
+// 1.0-2.0.cc:465-474, :62 and src/computefourier-3.0.cc:800-810), uploads
+// them, and launches the pipeline on the plan's stream.  No computation of
+// the transform happens on the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../include/sfft.h"
+#include "engine.h"
+#include "host_plan.h"
+
+#include <atomic>
+#include <deque>
+
+namespace sfft {
+static std::atomic<long> g_launches{0};
+void note_launches(long n) { g_launches += n; }
+void mark(StageEvents *se, cudaStream_t s) {
+  if (se && se->recorded < 8) cudaEventRecord(se->ev[se->recorded++], s);
+}
+}  // namespace sfft
+
+namespace {
+
+thread_local std::string g_err;
+
+void set_err(const std::string &m) { g_err = m; }
+
+bool cuda_ok(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return true;
+  set_err(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+
+// A device allocation owned by a plan.
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  bool ensure(size_t b) {
+    if (b <= bytes && p) return true;
+    release();
+    if (b == 0) b = 16;
+    if (cudaMalloc(&p, b) != cudaSuccess) {
+      cudaGetLastError();
+      set_err("device allocation of " + std::to_string(b) + " bytes failed");
+      p = nullptr;
+      return false;
+    }
+    bytes = b;
+    return true;
+  }
+  template <typename T>
+  bool upload(const std::vector<T> &v) {
+    if (!ensure(sizeof(T) * v.size())) return false;
+    return cuda_ok(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice), "upload");
+  }
+  template <typename T>
+  T *as() const {
+    return (T *)p;
+  }
+};
+
+int gcd_ref(int a, int b) { return (a % b == 0) ? b : gcd_ref(b, a % b); }  // src/utils.cc:41-46
+
+int mod_inverse_ref(int a, int n) {  // src/utils.cc:85-101
+  int i = n, v = 0, d = 1;
+  while (a > 0) {
+    int t = i / a, x = a;
+    a = i % x;
+    i = x;
+    x = d;
+    d = v - t * x;
+    v = x;
+  }
+  v %= n;
+  if (v < 0) v = (v + n) % n;
+  return v;
+}
+
+int ilog2(long v) {
+  int m = 0;
+  while ((1L << m) < v) m++;
+  return m;
+}
+
+std::vector<float> to_f32(const std::vector<double> &v) {
+  std::vector<float> o(v.size());
+  for (size_t i = 0; i < v.size(); i++) o[i] = (float)v[i];
+  return o;
+}
+
+}  // namespace
+
+struct PlanImpl {
+  int version = 0, n = 0, k = 0, prec = sfft::PREC_FP64, device = 0, max_batch = 16;
+  sfft::V12Params p12;
+  sfft::V3Params p3;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  std::mutex mu;
+  // constants
+  DBuf taps_a, taps_b, win_a, win_b, tw_a, tw_b, tw_c;
+  int win_half_a = 0, win_half_b = 0;
+  // workspace
+  int slots = 0;
+  DBuf xs, J, score, hits, comb_bits, comb_list, counters, out_idx, out_val;
+  DBuf man, g1, g2, perm, est_f, est_v, map_keys, map_vals, map_list;
+  DBuf rparams, inputs, dense_ptrs, in_stage, dense_stage, trace;
+  std::vector<unsigned> epoch;
+  int hit_cap = 0, out_cap = 0, est_cap = 0, map_cap = 0, table_cap = 0;
+  int rp_stride = 0;
+  std::vector<int> last_rp;  // draws of the last exec (slot 0)
+  // stage timing (sfft_profile): event sets of launches not yet harvested
+  bool profiling = false;
+  std::vector<sfft::StageEvents *> free_sets;
+  std::deque<sfft::StageEvents *> pending;
+  double stage_ms[8] = {0};
+  long profiled = 0;
+  ~PlanImpl() {
+    for (auto *e : free_sets) destroy(e);
+    for (auto *e : pending) destroy(e);
+  }
+  static void destroy(sfft::StageEvents *e) {
+    for (int i = 0; i < 8; i++) cudaEventDestroy(e->ev[i]);
+    delete e;
+  }
+  sfft::StageEvents *take_set() {
+    sfft::StageEvents *e;
+    if (!free_sets.empty()) {
+      e = free_sets.back();
+      free_sets.pop_back();
+    } else {
+      e = new sfft::StageEvents();
+      for (int i = 0; i < 8; i++) cudaEventCreate(&e->ev[i]);
+    }
+    e->recorded = 0;
+    return e;
+  }
+  void harvest() {
+    while (!pending.empty()) {
+      sfft::StageEvents *e = pending.front();
+      pending.pop_front();
+      if (e->recorded > 0 && cudaEventSynchronize(e->ev[e->recorded - 1]) == cudaSuccess) {
+        for (int i = 0; i + 1 < e->recorded; i++) {
+          float ms = 0;
+          if (cudaEventElapsedTime(&ms, e->ev[i], e->ev[i + 1]) == cudaSuccess) stage_ms[i] += ms;
+        }
+        profiled++;
+      }
+      free_sets.push_back(e);
+    }
+  }
+};
+
+namespace {
+
+int L12(const PlanImpl &P) { return P.p12.loops_loc + P.p12.loops_est; }
+
+// ------------------------------------------------------------- constants --
+
+bool upload_twiddles(DBuf &b, long N, int prec) {
+  const std::vector<double> &tw = sfft::fft_twiddles(N);
+  std::vector<double> t(tw.begin(), tw.begin() + 2 * N);
+  if (prec == sfft::PREC_FP64) return b.upload(t);
+  return b.upload(to_f32(t));
+}
+
+// Estimation window of a v1/v2 filter: the q = n/B entries of filter.freq
+// that src/computefourier-1.0-2.0.cc:370-385 can index, win[m] =
+// freq[(n - d) % n] with d = m - (q-1)/2.
+bool upload_v12_window(DBuf &b, const std::vector<double> &freq, int n, int q, int prec) {
+  if (prec == sfft::PREC_FP64) {
+    std::vector<double> w(4 * (size_t)q);
+    for (int m = 0; m < q; m++) {
+      const long d = m - (q - 1) / 2;
+      const long idx = ((long)n - d) % n;
+      const double c = freq[2 * idx], dd = freq[2 * idx + 1];
+      w[4 * m] = c;
+      w[4 * m + 1] = dd;
+      w[4 * m + 2] = c * c + dd * dd;  // same rounding as the reference's hadd
+      w[4 * m + 3] = 0.0;
+    }
+    return b.upload(w);
+  }
+  std::vector<float> w(2 * (size_t)q);
+  for (int m = 0; m < q; m++) {
+    const long d = m - (q - 1) / 2;
+    const long idx = ((long)n - d) % n;
+    const double c = freq[2 * idx], dd = freq[2 * idx + 1];
+    const double den = c * c + dd * dd;
+    w[2 * m] = (float)(c / den);
+    w[2 * m + 1] = (float)(dd / den);
+  }
+  return b.upload(w);
+}
+
+// v3 window: freq[(m - half) mod n] for m in [0, 2*half].
+bool upload_v3_window(DBuf &b, const std::vector<double> &freq, int n, int half) {
+  std::vector<double> w(2 * (size_t)(2 * half + 1));
+  for (int m = 0; m <= 2 * half; m++) {
+    const long idx = (((long)m - half) % n + n) % n;
+    w[2 * m] = freq[2 * idx];
+    w[2 * m + 1] = freq[2 * idx + 1];
+  }
+  return b.upload(w);
+}
+
+bool upload_taps(DBuf &b, const std::vector<double> &t, int prec) {
+  if (prec == sfft::PREC_FP64) return b.upload(t);
+  return b.upload(to_f32(t));
+}
+
+// ------------------------------------------------------------- workspace --
+
+bool ensure_slots(PlanImpl &P, int want) {
+  if (want <= P.slots) return true;
+  const size_t S = (size_t)want;
+  const size_t cs = P.prec == sfft::PREC_FP64 ? 16 : 8;
+  if (!P.counters.ensure(sizeof(int) * sfft::CNT_STRIDE * S)) return false;
+  if (!P.inputs.ensure(sizeof(void *) * S) || !P.dense_ptrs.ensure(sizeof(void *) * S)) return false;
+  if (P.version < 2) {
+    const auto &p = P.p12;
+    const int L = L12(P);
+    P.rp_stride = 2 * L + p.Comb_loops + 1;
+    const int q = P.n / p.B_loc;
+    P.hit_cap = P.version == 0
+                    ? (int)std::min<long>((long)P.n, ((long)p.loops_loc * p.B_thresh * q) / p.loops_thresh + 1)
+                    : 1;
+    const long comb_max = std::min<long>((long)p.W_Comb, (long)p.Comb_loops * p.B_thresh);
+    P.out_cap = P.version == 0 ? P.hit_cap : (int)(comb_max * (P.n / p.W_Comb));
+    if (!P.xs.ensure(cs * p.x_samp_size * S) || !P.J.ensure(sizeof(int) * L * p.B_thresh * S) ||
+        !P.hits.ensure(sizeof(int) * P.hit_cap * S) ||
+        !P.comb_bits.ensure(sizeof(unsigned) * ((p.W_Comb + 31) / 32) * S) ||
+        !P.comb_list.ensure(sizeof(int) * p.W_Comb * S) || !P.out_idx.ensure(sizeof(int) * P.out_cap * S) ||
+        !P.out_val.ensure(cs * P.out_cap * S))
+      return false;
+    // vote counters persist across execs (epoch-tagged); grow by copy-free realloc
+    DBuf fresh;
+    if (!fresh.ensure(sizeof(unsigned) * (size_t)P.n * S)) return false;
+    if (!cuda_ok(cudaMemset(fresh.p, 0, sizeof(unsigned) * (size_t)P.n * S), "memset")) return false;
+    std::swap(P.score.p, fresh.p);
+    std::swap(P.score.bytes, fresh.bytes);
+    P.epoch.assign(S, 0);
+  } else {
+    const auto &p = P.p3;
+    P.rp_stride = 5;
+    P.est_cap = std::max(p.W_Man, std::max(p.B_g1, p.B_g2));
+    P.map_cap = 4 * (p.W_Man + p.B_g1 + p.B_g2) + 8 * P.k;
+    P.table_cap = 1;
+    while (P.table_cap < 2 * P.map_cap) P.table_cap <<= 1;
+    P.out_cap = P.map_cap;
+    if (!P.man.ensure(32 * (size_t)p.W_Man * S) || !P.g1.ensure(32 * (size_t)p.B_g1 * S) ||
+        !P.g2.ensure(32 * (size_t)p.B_g2 * S) || !P.est_f.ensure(sizeof(int) * P.est_cap * S) ||
+        !P.est_v.ensure(16 * (size_t)P.est_cap * S) || !P.map_keys.ensure(sizeof(int) * P.table_cap * S) ||
+        !P.map_vals.ensure(16 * (size_t)P.table_cap * S) || !P.map_list.ensure(sizeof(int) * P.map_cap * S) ||
+        !P.out_idx.ensure(sizeof(int) * P.out_cap * S) || !P.out_val.ensure(16 * (size_t)P.out_cap * S) ||
+        !P.trace.ensure(sizeof(double) * 5 * (size_t)P.map_cap))
+      return false;
+  }
+  if (!P.rparams.ensure(sizeof(int) * P.rp_stride * S)) return false;
+  P.slots = want;
+  return true;
+}
+
+// ------------------------------------------------------------------ RNG --
+
+// Draws of one transform, in the reference's order.
+void draw_params(const PlanImpl &P, int *rp, unsigned epoch) {
+  const int n = P.n;
+  if (P.version < 2) {
+    const int L = L12(P);
+    for (int i = 0; i < L; i++) {  // src/computefourier-1.0-2.0.cc:465-474
+      int a = 0;
+      while (gcd_ref(a, n) != 1) a = (int)(random() % n);
+      rp[i] = a;
+      rp[L + i] = mod_inverse_ref(a, n);
+    }
+    for (int c = 0; c < P.p12.Comb_loops; c++) {  // :62, once per Comb_Filt call
+      if (P.version == 1) {
+        const int sigma = n / P.p12.W_Comb;
+        rp[2 * L + c] = (int)(unsigned)std::floor(drand48() * sigma);
+      } else {
+        rp[2 * L + c] = 0;
+      }
+    }
+    rp[2 * L + P.p12.Comb_loops] = (int)epoch;
+  } else {  // src/computefourier-3.0.cc:800-810
+    int a = 0;
+    while (gcd_ref(a, n) != 1) a = (int)(random() % n);
+    rp[0] = a;
+    rp[1] = mod_inverse_ref(a, n);
+    rp[2] = (int)(random() % n);
+    rp[3] = (int)(unsigned)std::floor(drand48() * n);
+    rp[4] = (int)(unsigned)std::floor(drand48() * n);
+  }
+}
+
+// ---------------------------------------------------------------- launch --
+
+sfft::V12Dev v12_view(PlanImpl &P) {
+  sfft::V12Dev d{};
+  const auto &p = P.p12;
+  d.version = P.version;
+  d.prec = P.prec;
+  d.n = P.n;
+  d.logn = ilog2(P.n);
+  d.k = P.k;
+  d.num = p.B_thresh;
+  d.B_loc = p.B_loc;
+  d.B_est = p.B_est;
+  d.L_loc = p.loops_loc;
+  d.L_est = p.loops_est;
+  d.L = L12(P);
+  d.thresh = p.loops_thresh;
+  d.W = p.W_Comb;
+  d.comb_loops = p.Comb_loops;
+  d.w_loc = p.w_loc;
+  d.w_est = p.w_est;
+  d.q_loc = P.n / p.B_loc;
+  d.q_est = P.n / p.B_est;
+  d.xs_size = p.x_samp_size;
+  d.taps_loc = P.taps_a.p;
+  d.taps_est = P.taps_b.p;
+  d.win_loc = P.win_a.p;
+  d.win_est = P.win_b.p;
+  d.tw_loc = P.tw_a.p;
+  d.tw_est = P.tw_b.p;
+  d.tw_comb = P.tw_c.p;
+  d.xs = P.xs.p;
+  d.J = P.J.as<int>();
+  d.score = P.score.as<unsigned>();
+  d.hits = P.hits.as<int>();
+  d.comb_bits = P.comb_bits.as<unsigned>();
+  d.comb_list = P.comb_list.as<int>();
+  d.counters = P.counters.as<int>();
+  d.out_idx = P.out_idx.as<int>();
+  d.out_val = P.out_val.p;
+  d.hit_cap = P.hit_cap;
+  d.out_cap = P.out_cap;
+  d.rparams = P.rparams.as<int>();
+  d.rp_stride = P.rp_stride;
+  d.inputs = (const void *const *)P.inputs.p;
+  return d;
+}
+
+sfft::V3Dev v3_view(PlanImpl &P) {
+  sfft::V3Dev d{};
+  const auto &p = P.p3;
+  d.prec = sfft::PREC_FP64;
+  d.n = P.n;
+  d.logn = ilog2(P.n);
+  d.k = P.k;
+  d.W = p.W_Man;
+  d.B1 = p.B_g1;
+  d.B2 = p.B_g2;
+  d.w1 = p.w_g1;
+  d.w2 = p.w_g2;
+  d.q1 = P.n / p.B_g1;
+  d.q2 = P.n / p.B_g2;
+  d.win1_half = P.win_half_a;
+  d.win2_half = P.win_half_b;
+  d.taps1 = P.taps_a.p;
+  d.taps2 = P.taps_b.p;
+  d.win1 = P.win_a.p;
+  d.win2 = P.win_b.p;
+  d.tw_man = P.tw_c.p;
+  d.tw_g1 = P.tw_a.p;
+  d.tw_g2 = P.tw_b.p;
+  d.man = P.man.p;
+  d.g1 = P.g1.p;
+  d.g2 = P.g2.p;
+  d.perm = P.perm.p;
+  d.est_f = P.est_f.as<int>();
+  d.est_v = P.est_v.p;
+  d.map_keys = P.map_keys.as<int>();
+  d.map_vals = P.map_vals.p;
+  d.map_table = P.map_list.as<int>();
+  d.est_cap = P.est_cap;
+  d.map_cap = P.map_cap;
+  d.table_cap = P.table_cap;
+  d.counters = P.counters.as<int>();
+  d.out_idx = P.out_idx.as<int>();
+  d.out_val = P.out_val.p;
+  d.out_cap = P.out_cap;
+  d.max_passes = 3000;
+  d.trace = P.trace.as<double>();
+  d.trace_cap = P.map_cap;
+  d.rparams = P.rparams.as<int>();
+  d.rp_stride = P.rp_stride;
+  d.inputs = (const void *const *)P.inputs.p;
+  return d;
+}
+
+// Uploads draws and input pointers for `num` slots and runs the pipeline.
+bool launch(PlanImpl &P, int num, const void *const *in_dev, int in_type, cudaStream_t s) {
+  std::vector<int> rp((size_t)P.rp_stride * num);
+  for (int i = 0; i < num; i++) {
+    unsigned ep = 0;
+    if (P.version < 2) {
+      if (++P.epoch[i] >= (1u << 24)) {  // wrap: clear this slot's vote counters
+        if (!cuda_ok(cudaMemsetAsync(P.score.as<unsigned>() + (size_t)i * P.n, 0, sizeof(unsigned) * P.n, s),
+                     "memset"))
+          return false;
+        P.epoch[i] = 1;
+      }
+      ep = P.epoch[i];
+    }
+    draw_params(P, &rp[(size_t)i * P.rp_stride], ep);
+  }
+  P.last_rp.assign(rp.begin(), rp.begin() + P.rp_stride);
+  // pageable sources: the runtime stages them before returning
+  if (!cuda_ok(cudaMemcpyAsync(P.rparams.p, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice, s),
+               "params upload"))
+    return false;
+  std::vector<const void *> ptrs(in_dev, in_dev + num);
+  if (!cuda_ok(cudaMemcpyAsync(P.inputs.p, ptrs.data(), sizeof(void *) * num, cudaMemcpyHostToDevice, s),
+               "pointer upload"))
+    return false;
+  sfft::StageEvents *se = P.profiling ? P.take_set() : nullptr;
+  bool ok;
+  if (P.version < 2) {
+    sfft::V12Dev d = v12_view(P);
+    d.in_type = in_type;
+    ok = cuda_ok(sfft::v12_run(d, num, s, se), "v1/v2 launch");
+  } else {
+    sfft::V3Dev d = v3_view(P);
+    d.in_type = in_type;
+    ok = cuda_ok(sfft::v3_run(d, num, s, se), "v3 launch");
+  }
+  if (se) P.pending.push_back(se);
+  return ok;
+}
+
+bool check_device_errors(PlanImpl &P, int num) {
+  std::vector<int> cnt((size_t)sfft::CNT_STRIDE * num);
+  if (!cuda_ok(cudaMemcpy(cnt.data(), P.counters.p, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost),
+               "counters"))
+    return false;
+  for (int i = 0; i < num; i++) {
+    const int e = cnt[(size_t)i * sfft::CNT_STRIDE + sfft::CNT_ERR];
+    if (e) {
+      char buf[160];
+      std::snprintf(buf, sizeof buf, "device reported error bits 0x%x on signal %d (1 hits, 2 output, 4 v3 no fixpoint, 8 v3 capacity)",
+                    e, i);
+      set_err(buf);
+      return false;
+    }
+  }
+  return true;
+}
+
+bool is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+std::mutex g_alloc_mu;
+std::set<void *> g_pinned;
+
+PlanImpl *impl(sfft_plan *p) { return p ? (PlanImpl *)p->data : nullptr; }
+
+// Runs `num` (<= slots) transforms whose inputs are host or device
+// pointers and writes dense n-point outputs (host or device).
+bool exec_dense_chunk(PlanImpl &P, int num, complex_t **in, complex_t **out) {
+  cudaStream_t s = P.stream;
+  const size_t nb = sizeof(double) * 2 * (size_t)P.n;
+  std::vector<const void *> dev_in(num);
+  bool need_in_stage = false, need_out_stage = false;
+  for (int i = 0; i < num; i++) {
+    if (!is_device_ptr(in[i])) need_in_stage = true;
+    if (!is_device_ptr(out[i])) need_out_stage = true;
+  }
+  if (need_in_stage && !P.in_stage.ensure(nb * P.slots)) return false;
+  if (need_out_stage && !P.dense_stage.ensure(nb * P.slots)) return false;
+  for (int i = 0; i < num; i++) {
+    if (is_device_ptr(in[i])) {
+      dev_in[i] = in[i];
+    } else {
+      void *dst = (char *)P.in_stage.p + nb * i;
+      if (!cuda_ok(cudaMemcpyAsync(dst, in[i], nb, cudaMemcpyHostToDevice, s), "input copy")) return false;
+      dev_in[i] = dst;
+    }
+  }
+  if (!launch(P, num, dev_in.data(), sfft::IN_C128, s)) return false;
+  std::vector<void *> dense(num);
+  for (int i = 0; i < num; i++) {
+    dense[i] = is_device_ptr(out[i]) ? (void *)out[i] : (char *)P.dense_stage.p + nb * i;
+    if (!cuda_ok(cudaMemsetAsync(dense[i], 0, nb, s), "output clear")) return false;
+  }
+  if (!cuda_ok(cudaMemcpyAsync(P.dense_ptrs.p, dense.data(), sizeof(void *) * num, cudaMemcpyHostToDevice, s),
+               "pointer upload"))
+    return false;
+  if (!cuda_ok(sfft::scatter_dense(P.out_idx.as<int>(), P.out_val.p, P.version < 2 ? P.prec : sfft::PREC_FP64,
+                                   P.counters.as<int>(), P.out_cap, (void *const *)P.dense_ptrs.p, num, s),
+               "scatter"))
+    return false;
+  for (int i = 0; i < num; i++)
+    if (!is_device_ptr(out[i]) &&
+        !cuda_ok(cudaMemcpyAsync(out[i], dense[i], nb, cudaMemcpyDeviceToHost, s), "output copy"))
+      return false;
+  if (!cuda_ok(cudaStreamSynchronize(s), "exec")) return false;
+  return check_device_errors(P, num);
+}
+
+}  // namespace
+
+// =================================================================== C API
+
+extern "C" {
+
+void *sfft_malloc(size_t s) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, s ? s : 16) == cudaSuccess) {
+    std::lock_guard<std::mutex> g(g_alloc_mu);
+    g_pinned.insert(p);
+    return p;
+  }
+  cudaGetLastError();
+  if (posix_memalign(&p, 64, s ? s : 16)) return nullptr;  // memory only, no compute
+  return p;
+}
+
+void sfft_free(void *p) {
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> g(g_alloc_mu);
+    auto it = g_pinned.find(p);
+    if (it != g_pinned.end()) {
+      g_pinned.erase(it);
+      cudaFreeHost(p);
+      return;
+    }
+  }
+  free(p);
+}
+
+const char *sfft_last_error(void) { return g_err.c_str(); }
+
+sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_optimization,
+                             const sfft_options *opt) {
+  (void)fftw_optimization;
+  g_err.clear();
+  if (version != SFFT_VERSION_1 && version != SFFT_VERSION_2 && version != SFFT_VERSION_3) {
+    set_err("unknown sFFT version");
+    return nullptr;
+  }
+  if (n < 16 || (n & (n - 1)) || k < 1 || n > (1 << 30)) {
+    set_err("n must be a power of two in [16, 2^30] and k >= 1");
+    return nullptr;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_err("no CUDA device: the GB300 sFFT engine has no CPU path");
+    return nullptr;
+  }
+  std::unique_ptr<PlanImpl> P(new (std::nothrow) PlanImpl());
+  if (!P) {
+    set_err("out of host memory");
+    return nullptr;
+  }
+  P->version = (int)version;
+  P->n = n;
+  P->k = k;
+  if (opt) {
+    P->prec = opt->precision == SFFT_PREC_FP32 ? sfft::PREC_FP32 : sfft::PREC_FP64;
+    if (opt->max_batch > 0) P->max_batch = opt->max_batch;
+  }
+  if (P->version == 2) P->prec = sfft::PREC_FP64;  // phase-slope decoding needs FP64
+  if (opt && opt->device >= 0) {
+    if (!cuda_ok(cudaSetDevice(opt->device), "cudaSetDevice")) return nullptr;
+  }
+  cudaGetDevice(&P->device);
+  std::string err;
+  sfft::HostFilter fa, fb;
+  if (P->version < 2) {
+    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, P->version == 1, P->p12, fa, fb, err)) {
+      set_err(err);
+      return nullptr;
+    }
+    const auto &p = P->p12;
+    const int mx = sfft::v12_max_fft(P->prec);
+    if (p.B_loc > mx || p.B_est > mx || (P->version == 1 && p.W_Comb > mx)) {
+      set_err("bucket FFT longer than " + std::to_string(mx) + " points is not supported by this build");
+      return nullptr;
+    }
+    if (L12(*P) > 32) {
+      set_err("more than 32 loops is not supported by this build");
+      return nullptr;
+    }
+    if (!upload_taps(P->taps_a, fa.time, P->prec) || !upload_taps(P->taps_b, fb.time, P->prec) ||
+        !upload_v12_window(P->win_a, fa.freq, n, n / p.B_loc, P->prec) ||
+        !upload_v12_window(P->win_b, fb.freq, n, n / p.B_est, P->prec) ||
+        !upload_twiddles(P->tw_a, p.B_loc, P->prec) || !upload_twiddles(P->tw_b, p.B_est, P->prec) ||
+        !upload_twiddles(P->tw_c, std::max(p.W_Comb, 2), P->prec))
+      return nullptr;
+  } else {
+    if (sfft::build_v3_plan((unsigned)n, (unsigned)k, P->p3, fa, fb, err)) {
+      set_err(err);
+      return nullptr;
+    }
+    const auto &p = P->p3;
+    if (p.W_Man > 8192 || p.B_g1 > 8192) {
+      set_err("v3 comb wider than 8192 buckets is not supported by this build");
+      return nullptr;
+    }
+    P->win_half_a = 3 * (n / p.B_g1) / 2 + 2;
+    P->win_half_b = 3 * (n / p.B_g2) / 2 + 2;
+    if (2 * P->win_half_a + 1 > n) P->win_half_a = (n - 1) / 2;
+    if (2 * P->win_half_b + 1 > n) P->win_half_b = (n - 1) / 2;
+    if (!P->taps_a.upload(fa.time) || !P->taps_b.upload(fb.time) ||
+        !upload_v3_window(P->win_a, fa.freq, n, P->win_half_a) ||
+        !upload_v3_window(P->win_b, fb.freq, n, P->win_half_b) ||
+        !upload_twiddles(P->tw_a, p.B_g1, sfft::PREC_FP64) || !upload_twiddles(P->tw_b, p.B_g2, sfft::PREC_FP64) ||
+        !upload_twiddles(P->tw_c, p.W_Man, sfft::PREC_FP64))
+      return nullptr;
+  }
+  if (!cuda_ok(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking), "stream")) return nullptr;
+  if (!cuda_ok(cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming), "event")) return nullptr;
+  if (!ensure_slots(*P, 1)) return nullptr;
+  sfft_plan *plan = (sfft_plan *)std::malloc(sizeof(sfft_plan));
+  if (!plan) {
+    set_err("out of host memory");
+    return nullptr;
+  }
+  plan->version = version;
+  plan->n = (unsigned)n;
+  plan->k = (unsigned)k;
+  plan->data = P.release();
+  return plan;
+}
+
+sfft_plan *sfft_make_plan(int n, int k, enum sfft_version version, int fftw_optimization) {
+  return sfft_make_plan_ex(n, k, version, fftw_optimization, nullptr);
+}
+
+void sfft_free_plan(sfft_plan *plan) {
+  if (!plan) return;
+  PlanImpl *P = impl(plan);
+  if (P) {
+    if (P->stream) {
+      cudaStreamSynchronize(P->stream);
+      cudaStreamDestroy(P->stream);
+    }
+    if (P->done) cudaEventDestroy(P->done);
+    delete P;
+  }
+  std::free(plan);
+}
+
+long sfft_output_capacity(const sfft_plan *plan) {
+  const PlanImpl *P = plan ? (const PlanImpl *)plan->data : nullptr;
+  if (!P) {
+    set_err("null plan");
+    return -1;
+  }
+  return P->out_cap;
+}
+
+void sfft_exec(sfft_plan *plan, complex_t *in, complex_t *out) {
+  sfft_exec_many(plan, 1, &in, &out);
+}
+
+void sfft_exec_many(sfft_plan *plan, int num, complex_t **in, complex_t **out) {
+  PlanImpl *P = impl(plan);
+  if (!P || num < 0 || (num && (!in || !out))) {
+    set_err("invalid arguments");
+    return;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  cudaSetDevice(P->device);
+  g_err.clear();
+  const int chunk = std::max(1, std::min(P->max_batch, num));
+  if (!ensure_slots(*P, chunk)) return;
+  for (int i = 0; i < num; i += chunk) {
+    const int m = std::min(chunk, num - i);
+    if (!exec_dense_chunk(*P, m, in + i, out + i)) return;
+  }
+}
+
+long sfft_exec_sparse(sfft_plan *plan, const complex_t *in, int *out_idx, complex_t *out_val, long cap) {
+  PlanImpl *P = impl(plan);
+  if (!P || !in || !out_idx || !out_val) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  cudaSetDevice(P->device);
+  g_err.clear();
+  cudaStream_t s = P->stream;
+  const size_t nb = sizeof(double) * 2 * (size_t)P->n;
+  const void *dev_in = in;
+  if (!is_device_ptr(in)) {
+    if (!P->in_stage.ensure(nb * std::max(1, P->slots))) return -1;
+    if (!cuda_ok(cudaMemcpyAsync(P->in_stage.p, in, nb, cudaMemcpyHostToDevice, s), "input copy")) return -1;
+    dev_in = P->in_stage.p;
+  }
+  if (!launch(*P, 1, &dev_in, sfft::IN_C128, s)) return -1;
+  int cnt[sfft::CNT_STRIDE];
+  if (!cuda_ok(cudaMemcpyAsync(cnt, P->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, s), "count") ||
+      !cuda_ok(cudaStreamSynchronize(s), "exec"))
+    return -1;
+  if (cnt[sfft::CNT_ERR]) {
+    check_device_errors(*P, 1);
+    return -1;
+  }
+  const long c = cnt[sfft::CNT_OUT];
+  if (c > cap) {
+    set_err("output capacity too small (" + std::to_string(c) + " coefficients)");
+    return -1;
+  }
+  const bool dev_out = is_device_ptr(out_idx);
+  const cudaMemcpyKind kind = dev_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (!cuda_ok(cudaMemcpyAsync(out_idx, P->out_idx.p, sizeof(int) * c, kind, s), "index copy")) return -1;
+  const bool fp32_vals = P->version < 2 && P->prec == sfft::PREC_FP32;
+  if (!fp32_vals) {
+    if (!cuda_ok(cudaMemcpyAsync(out_val, P->out_val.p, 16 * c, kind, s), "value copy")) return -1;
+    if (!cuda_ok(cudaStreamSynchronize(s), "copy")) return -1;
+  } else {
+    std::vector<float> tmp(2 * (size_t)c);
+    if (!cuda_ok(cudaMemcpyAsync(tmp.data(), P->out_val.p, 8 * c, cudaMemcpyDeviceToHost, s), "value copy") ||
+        !cuda_ok(cudaStreamSynchronize(s), "copy"))
+      return -1;
+    std::vector<double> w(2 * (size_t)c);
+    for (size_t i = 0; i < w.size(); i++) w[i] = tmp[i];
+    if (!cuda_ok(cudaMemcpy(out_val, w.data(), 16 * c, dev_out ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost),
+                 "value copy"))
+      return -1;
+  }
+  return c;
+}
+
+int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type, int *out_idx, void *out_val,
+                    int *out_count, long out_stride, void *stream) {
+  PlanImpl *P = impl(plan);
+  if (!P || num < 1 || !in || !out_idx || !out_val || !out_count || out_stride < 0) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  if (out_stride < P->out_cap) {
+    set_err("out_stride below sfft_output_capacity");
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  cudaSetDevice(P->device);
+  g_err.clear();
+  cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
+  if (!ensure_slots(*P, std::min(num, std::max(P->max_batch, num)))) return -1;
+  if (!cuda_ok(cudaStreamWaitEvent(s, P->done, 0), "event wait")) return -1;
+  const size_t cs = (P->version < 2 && P->prec == sfft::PREC_FP32) ? 8 : 16;
+  for (int i0 = 0; i0 < num; i0 += P->slots) {
+    const int m = std::min(P->slots, num - i0);
+    if (!launch(*P, m, in + i0, in_type, s)) return -1;
+    // gather per-slot results into the caller's strided buffers
+    for (int i = 0; i < m; i++) {
+      if (!cuda_ok(cudaMemcpyAsync(out_count + i0 + i, P->counters.as<int>() + i * sfft::CNT_STRIDE + sfft::CNT_OUT,
+                                   sizeof(int), cudaMemcpyDeviceToDevice, s),
+                   "count copy"))
+        return -1;
+    }
+    if (!cuda_ok(cudaMemcpy2DAsync(out_idx + (size_t)i0 * out_stride, sizeof(int) * out_stride, P->out_idx.p,
+                                   sizeof(int) * P->out_cap, sizeof(int) * P->out_cap, m, cudaMemcpyDeviceToDevice, s),
+                 "index copy") ||
+        !cuda_ok(cudaMemcpy2DAsync((char *)out_val + cs * (size_t)i0 * out_stride, cs * out_stride, P->out_val.p,
+                                   cs * P->out_cap, cs * P->out_cap, m, cudaMemcpyDeviceToDevice, s),
+                 "value copy"))
+      return -1;
+  }
+  return cuda_ok(cudaEventRecord(P->done, s), "event") ? 0 : -1;
+}
+
+int sfft_sync(sfft_plan *plan) {
+  PlanImpl *P = impl(plan);
+  if (!P) {
+    set_err("null plan");
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  if (!cuda_ok(cudaEventSynchronize(P->done), "sync") || !cuda_ok(cudaStreamSynchronize(P->stream), "sync"))
+    return -1;
+  return check_device_errors(*P, std::max(1, P->slots)) ? 0 : -1;
+}
+
+long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap) {
+  PlanImpl *P = impl(plan);
+  if (!P || !dst) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  if (!cuda_ok(cudaStreamSynchronize(P->stream), "sync")) return -1;
+  auto fetch = [&](const void *src, long count, size_t esz) -> long {
+    if (count > cap) {
+      set_err("debug buffer too small");
+      return -1;
+    }
+    if (!cuda_ok(cudaMemcpy(dst, src, esz * count, cudaMemcpyDeviceToHost), "debug copy")) return -1;
+    return count;
+  };
+  if (P->version < 2) {
+    const auto &p = P->p12;
+    const int L = L12(*P);
+    switch (what) {
+      case 0: {
+        if (2 * L > cap) return -1;
+        std::memcpy(dst, P->last_rp.data(), sizeof(int) * 2 * L);
+        return 2 * L;
+      }
+      case 1:
+        return fetch(P->J.p, (long)L * p.B_thresh, sizeof(int));
+      case 2: {
+        if (P->n > cap) return -1;
+        std::vector<unsigned> raw(P->n);
+        if (!cuda_ok(cudaMemcpy(raw.data(), P->score.p, sizeof(unsigned) * P->n, cudaMemcpyDeviceToHost), "debug"))
+          return -1;
+        int *o = (int *)dst;
+        for (int i = 0; i < P->n; i++) o[i] = ((raw[i] >> 8) == P->epoch[0]) ? (int)(raw[i] & 255u) : 0;
+        return P->n;
+      }
+      case 3:
+        return fetch(P->xs.p, p.x_samp_size, P->prec == sfft::PREC_FP64 ? 16 : 8);
+      case 4: {
+        int cnt[sfft::CNT_STRIDE];
+        if (!cuda_ok(cudaMemcpy(cnt, P->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost), "debug")) return -1;
+        return fetch(P->comb_list.p, cnt[sfft::CNT_COMB], sizeof(int));
+      }
+      default:
+        break;
+    }
+  } else if (what == 6) {
+    int cnt[sfft::CNT_STRIDE];
+    if (!cuda_ok(cudaMemcpy(cnt, P->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost), "debug")) return -1;
+    const long nrec = std::min(cnt[sfft::CNT_TRACE], P->map_cap);
+    if (5 * nrec > cap) return -1;
+    if (!cuda_ok(cudaMemcpy(dst, P->trace.p, sizeof(double) * 5 * nrec, cudaMemcpyDeviceToHost), "debug"))
+      return -1;
+    return 5 * nrec;
+  } else if (what == 5) {
+    int cnt[sfft::CNT_STRIDE];
+    if (!cuda_ok(cudaMemcpy(cnt, P->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost), "debug")) return -1;
+    if (cap < 1) return -1;
+    ((int *)dst)[0] = cnt[sfft::CNT_V3];
+    return 1;
+  } else if (what == 0) {
+    if (cap < 5) return -1;
+    std::memcpy(dst, P->last_rp.data(), sizeof(int) * 5);
+    return 5;
+  }
+  set_err("unknown diagnostic");
+  return -1;
+}
+
+int sfft_describe_plan(int n, int k, enum sfft_version version, long *fields, int nfields) {
+  g_err.clear();
+  if (!fields || n < 16 || (n & (n - 1)) || k < 1) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  std::string err;
+  sfft::HostFilter fa, fb;
+  std::vector<long> v;
+  if (version == SFFT_VERSION_1 || version == SFFT_VERSION_2) {
+    sfft::V12Params p;
+    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, version == SFFT_VERSION_2, p, fa, fb, err)) {
+      set_err(err);
+      return -1;
+    }
+    v = {p.B_loc, p.B_thresh, p.B_est, p.W_Comb, p.Comb_loops, p.loops_loc, p.loops_thresh, p.loops_est,
+         p.w_loc, p.w_est, p.x_samp_size};
+  } else if (version == SFFT_VERSION_3) {
+    sfft::V3Params p;
+    if (sfft::build_v3_plan((unsigned)n, (unsigned)k, p, fa, fb, err)) {
+      set_err(err);
+      return -1;
+    }
+    v = {p.W_Man, p.B_g1, p.w_g1, p.B_g2, p.w_g2};
+  } else {
+    set_err("unknown sFFT version");
+    return -1;
+  }
+  const int m = std::min<int>(nfields, (int)v.size());
+  for (int i = 0; i < m; i++) fields[i] = v[i];
+  return m;
+}
+
+int sfft_describe_filter(int n, int k, enum sfft_version version, int which, double *time, long time_cap,
+                         double *freq, long freq_cap) {
+  g_err.clear();
+  if (n < 16 || (n & (n - 1)) || k < 1 || (which != 0 && which != 1)) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  std::string err;
+  sfft::HostFilter fa, fb;
+  int rc;
+  if (version == SFFT_VERSION_1 || version == SFFT_VERSION_2) {
+    sfft::V12Params p;
+    rc = sfft::build_v12_plan((unsigned)n, (unsigned)k, version == SFFT_VERSION_2, p, fa, fb, err);
+  } else if (version == SFFT_VERSION_3) {
+    sfft::V3Params p;
+    rc = sfft::build_v3_plan((unsigned)n, (unsigned)k, p, fa, fb, err);
+  } else {
+    set_err("unknown sFFT version");
+    return -1;
+  }
+  if (rc) {
+    set_err(err);
+    return -1;
+  }
+  const sfft::HostFilter &f = which ? fb : fa;
+  if (time) {
+    if (time_cap < 2L * f.w) {
+      set_err("time buffer too small");
+      return -1;
+    }
+    std::memcpy(time, f.time.data(), sizeof(double) * 2 * f.w);
+  }
+  if (freq) {
+    if (freq_cap < 2L * n) {
+      set_err("freq buffer too small");
+      return -1;
+    }
+    std::memcpy(freq, f.freq.data(), sizeof(double) * 2 * (size_t)n);
+  }
+  return f.w;
+}
+
+int sfft_profile(sfft_plan *plan, int enable) {
+  PlanImpl *P = impl(plan);
+  if (!P) {
+    set_err("null plan");
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  P->harvest();
+  P->profiling = enable != 0;
+  for (double &m : P->stage_ms) m = 0;
+  P->profiled = 0;
+  return 0;
+}
+
+long sfft_profile_read(sfft_plan *plan, double *stage_ms, int nstage) {
+  PlanImpl *P = impl(plan);
+  if (!P || !stage_ms) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  P->harvest();
+  for (int i = 0; i < nstage && i < 8; i++) stage_ms[i] = P->stage_ms[i];
+  return P->profiled;
+}
+
+long sfft_kernel_launches(void) { return sfft::g_launches.load(); }
+
+}  // extern "C"

@@ -261,9 +261,13 @@ __device__ void block_top_indices(const K *keys, int N, int num, int *__restrict
   for (int i = lo; i < hi; i++) {
     K k = keys[i];
     if (k > cutoff) {
-      out[pos++] = i;
+      if (pos < num) out[pos] = i;
+      pos++;
     } else if (k == cutoff) {
-      if (eqr < need) out[pos++] = i;
+      if (eqr < need) {
+        if (pos < num) out[pos] = i;
+        pos++;
+      }
       eqr++;
     }
   }

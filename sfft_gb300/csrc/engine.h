@@ -1,0 +1,109 @@
+// engine.h — device-side view of a plan and the launch entry points of the
+// sFFT kernels.  Shared by the C-ABI layer (api.cc) and the kernels
+// (v12.cu, v3.cu).  Plain structs of device pointers and sizes.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sfft {
+
+// Optional per-stage timing: when non-null, an event is recorded on the
+// stream before the first stage and after each stage (stage names in
+// api.cc).  Kernel launches are counted in `launches`.
+struct StageEvents {
+  cudaEvent_t ev[8];
+  int recorded = 0;
+};
+void note_launches(long n);
+void mark(StageEvents *se, cudaStream_t s);
+
+enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
+enum InType { IN_C128 = 0, IN_C64 = 1 };
+
+// Per-slot counters (one block of ints per slot, zeroed before each exec).
+enum Counter { CNT_HITS = 0, CNT_COMB = 1, CNT_OUT = 2, CNT_ERR = 3, CNT_VOTED = 4, CNT_V3 = 5,
+               CNT_TRACE = 6, CNT_STRIDE = 16 };
+
+// Error bits reported in counters[CNT_ERR].
+enum ErrBits { ERR_HIT_OVERFLOW = 1, ERR_OUT_OVERFLOW = 2, ERR_V3_NOCONVERGE = 4, ERR_V3_CAP = 8 };
+
+// ---------------------------------------------------------------- v1/v2 --
+struct V12Dev {
+  int version;  // 0 = v1, 1 = v2
+  int prec;
+  int n, logn, k, num;
+  int B_loc, B_est, L_loc, L_est, L, thresh;
+  int W, comb_loops;
+  int w_loc, w_est;
+  int q_loc, q_est;  // n / B
+  long xs_size;      // per slot, complex entries
+  // plan constants
+  const void *taps_loc, *taps_est;  // w complex (double2 or float2)
+  const void *win_loc, *win_est;    // q entries: FP64 double4 (c, d, c^2+d^2, 0); FP32 float2 (g)
+  const void *tw_loc, *tw_est, *tw_comb;  // twiddle tables (double2 or float2)
+  // per-slot workspace
+  void *xs;                 // xs_size complex per slot
+  int *J;                   // L * num per slot
+  unsigned *score;          // n per slot: (epoch << 8) | votes
+  int *hits;                // hit_cap per slot
+  unsigned *comb_bits;      // W/32 per slot
+  int *comb_list;           // W per slot
+  int *counters;            // CNT_STRIDE per slot
+  int *out_idx;             // out_cap per slot
+  void *out_val;            // out_cap complex per slot (R2)
+  int hit_cap, out_cap;
+  // per-exec inputs
+  const int *rparams;       // per slot: a[L], ai[L], comb_offsets[comb_loops], epoch
+  int rp_stride;
+  const void *const *inputs;  // device array of per-slot input pointers
+  int in_type;
+};
+
+// Launches the whole v1/v2 pipeline for `nslots` signals on `stream`.
+cudaError_t v12_run(const V12Dev &d, int nslots, cudaStream_t stream, StageEvents *se = nullptr);
+// Scatters the sparse result of each slot into dense n-point complex128
+// outputs (device array of per-slot pointers, already zeroed).
+cudaError_t scatter_dense(const int *out_idx, const void *out_val, int prec, const int *counters,
+                          int out_cap, void *const *dense, int nslots, cudaStream_t stream);
+
+// Maximum bucket-FFT length held in one CTA's shared memory.
+int v12_max_fft(int prec);
+
+// -------------------------------------------------------------------- v3 --
+struct V3Dev {
+  int prec;
+  int n, logn, k;
+  int W, B1, B2, w1, w2;
+  int q1, q2;          // n / B1, n / B2
+  int win1_half, win2_half;
+  const void *taps1, *taps2;    // double2
+  const void *win1, *win2;      // double2, 2*half+1 entries centred on freq index 0
+  const void *tw_man, *tw_g1, *tw_g2;
+  // per-slot workspace
+  void *man;     // 2W complex (interleaved loops)
+  void *g1;      // 2*B1 complex
+  void *g2;      // 2*B2 complex
+  void *perm;    // (w2 + 1) complex
+  int *est_f;    // cap per slot
+  void *est_v;   // cap complex per slot
+  int *map_keys; // map_cap per slot
+  void *map_vals;
+  int *map_table;  // table_cap per slot
+  int est_cap, map_cap, table_cap;
+  int *counters;
+  int *out_idx;
+  void *out_val;
+  int out_cap;
+  int max_passes;
+  double *trace;       // slot 0 only: (round, stage, key, re, im) per estimate
+  int trace_cap;
+  const int *rparams;  // per slot: a, ai, b, init_offset, init_G_offset
+  int rp_stride;
+  const void *const *inputs;
+  int in_type;
+};
+
+cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t stream, StageEvents *se = nullptr);
+
+}  // namespace sfft

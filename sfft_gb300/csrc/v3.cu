@@ -1,0 +1,496 @@
+// v3.cu — the sFFT v3 ("exactly sparse") exec path on GB300.
+//
+//   k_v3_filters  six CTAs per signal: the two Mansour comb samplings
+//                 (computefourier-3.0.cc:96-127), the two shifts of the
+//                 contiguous Gaussian fold (:130-212) and of the permuted
+//                 Gaussian fold (:215-297), each followed by its
+//                 shared-memory FFT.  The permutation phase of the second
+//                 fold is e^{2 pi i ((b * idx) mod n) / n} from the exact
+//                 integer product, not the reference's running product
+//                 (:66-87); both describe the same phase.
+//   k_v3_peel     one CTA per signal runs alternate_fft's estimate / peel
+//                 rounds (:784-1088): bucket estimation in parallel,
+//                 subtraction of recovered tones with FP64 atomics, and the
+//                 bucket-count fixpoint test, with a bounded number of rounds.
+// The result map is a per-signal open-addressing table in global memory.
+// FP64 throughout: the phase-slope frequency decode needs phase accuracy
+// below pi/n.
+#include "common.cuh"
+#include "engine.h"
+
+namespace sfft {
+
+static constexpr double kPi = 3.14159265358979323846;
+
+__device__ __forceinline__ double2 ld_x(const void *base, int in_type, long i) {
+  if (in_type == IN_C128) return __ldg((const double2 *)base + i);
+  const float2 v = __ldg((const float2 *)base + i);
+  return make_double2((double)v.x, (double)v.y);
+}
+
+// --------------------------------------------------------------- filters --
+
+template <int PER>
+__global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *buf = (double2 *)smem_raw;
+  const int role = blockIdx.x, slot = blockIdx.y, l = role & 1;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const unsigned long long mask = (unsigned long long)d.n - 1;
+  const void *x = d.inputs[slot];
+  int N;
+  const double2 *tw;
+  double2 *dst;
+  if (role < 2) {  // Mansour: x[(init_offset + l + i * n/W) mod n]
+    N = d.W;
+    tw = (const double2 *)d.tw_man;
+    dst = (double2 *)d.man + (long)slot * 2 * d.W;
+    const long sigma = d.n / d.W;
+    const long o = rp[3] + l;
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      buf[i] = ld_x(x, d.in_type, (long)((unsigned long long)(o + i * sigma) & mask));
+  } else if (role < 4) {  // Gaussian 1: taps over x[init_G_offset + l + t]
+    N = d.B1;
+    tw = (const double2 *)d.tw_g1;
+    dst = (double2 *)d.g1 + (long)slot * 2 * d.B1;
+    const int chunks = d.w1 / d.B1;
+    const long base = (long)rp[4] + l;
+    const double2 *taps = (const double2 *)d.taps1;
+    for (int b = threadIdx.x; b < N; b += blockDim.x) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int c = 0; c < chunks; c++) {
+        const int t = c * N + b;
+        const double2 xv = ld_x(x, d.in_type, (long)((unsigned long long)(base + t) & mask));
+        acc = cadd<double>(acc, cmul<double>(xv, __ldg(taps + t)));
+      }
+      buf[b] = acc;
+    }
+  } else {  // Gaussian 2 on the permuted, phase-shifted samples
+    N = d.B2;
+    tw = (const double2 *)d.tw_g2;
+    dst = (double2 *)d.g2 + (long)slot * 2 * d.B2;
+    const int chunks = d.w2 / d.B2;
+    const unsigned long long ig = (unsigned)rp[4], ai = (unsigned)rp[1], bb = (unsigned)rp[2];
+    const double2 *taps = (const double2 *)d.taps2;
+    for (int b = threadIdx.x; b < N; b += blockDim.x) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int c = 0; c < chunks; c++) {
+        const int t = c * N + b;
+        const unsigned long long idx = (ig + (unsigned long long)(t + l) * ai) & mask;
+        const unsigned long long ph = (bb * idx) & mask;
+        double s, co;
+        sincos((2.0 * kPi * (double)ph) / (double)d.n, &s, &co);
+        const double2 pv = cmul<double>(ld_x(x, d.in_type, (long)idx), make_double2(co, s));
+        acc = cadd<double>(acc, cmul<double>(pv, __ldg(taps + t)));
+      }
+      buf[b] = acc;
+    }
+  }
+  __syncthreads();
+  block_fft<double, PER>(buf, N, 31 - __clz(N), tw);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) dst[2 * i + l] = buf[i];
+}
+
+// ------------------------------------------------------------------ peel --
+
+struct PeelCtx {
+  const V3Dev *d;
+  int n, n1;
+  double2 *man, *g1, *g2;
+  int *tkey;
+  double2 *tval;
+  int *list;
+  int tmask;
+  int *est_f;
+  double2 *est_v;
+  int a, ai, b, io, ig, aG, shift;
+};
+
+__device__ __forceinline__ double2 win_at(const double2 *win, int half, int n, int dist, int *err) {
+  int ds = dist >= (n >> 1) ? dist - n : dist;
+  if (ds < -half || ds > half) {
+    atomicOr(err, ERR_V3_CAP);
+    ds = ds < -half ? -half : half;
+  }
+  return __ldg(win + ds + half);
+}
+
+__device__ __forceinline__ int wrapmul(int x, int y) { return (int)((unsigned)x * (unsigned)y); }
+
+// Subtract a recovered tone from the three nearest buckets of both shifts
+// of a Gaussian filter (computefourier-3.0.cc:354-463).
+__device__ void update_gauss(const PeelCtx &c, double2 *SAMP, const double2 *win, int half, int B,
+                             int key, double2 v, int offset, int step, int *err) {
+  const int n = c.n, n1 = c.n1;
+  const unsigned q = n / B;
+  const int h = (int)(key * 1. / q + 0.5) % B;
+  const int dist1 = (int)(((unsigned)h * q - (unsigned)key + (unsigned)n) & (unsigned)n1);
+  const int dist2 = (int)(((unsigned)dist1 + (unsigned)n + q) & (unsigned)n1);
+  const int dist3 = (int)(((unsigned)dist1 + 2u * (unsigned)n - q) & (unsigned)n1);
+  const int ko1 = wrapmul(key, offset) % n;
+  const int ko2 = wrapmul(key, (int)((unsigned)offset + (unsigned)step)) % n;
+  const double PI2_DIV_N = 2 * kPi / n;
+  double s1, c1, s2, c2;
+  sincos(PI2_DIV_N * ko1, &s1, &c1);
+  sincos(PI2_DIV_N * ko2, &s2, &c2);
+  const double2 v1 = cmul<double>(v, make_double2(c1, s1));
+  const double2 v2 = cmul<double>(v, make_double2(c2, s2));
+  const int dists[3] = {dist1, dist2, dist3};
+  const int bks[3] = {h, (h + 1) % B, (h + B - 1) % B};
+#pragma unroll
+  for (int qd = 0; qd < 3; qd++) {
+    const double2 f = win_at(win, half, n, dists[qd], err);
+    const double2 r1 = cmul<double>(v1, f), r2 = cmul<double>(v2, f);
+    double *p0 = (double *)&SAMP[2 * bks[qd]];
+    double *p1 = (double *)&SAMP[2 * bks[qd] + 1];
+    atomicAdd(p0, -r1.x);
+    atomicAdd(p0 + 1, -r1.y);
+    atomicAdd(p1, -r2.x);
+    atomicAdd(p1 + 1, -r2.y);
+  }
+}
+
+// (computefourier-3.0.cc:300-351)
+__device__ void update_mansour(const PeelCtx &c, int key, double2 v) {
+  const int W = c.d->W;
+  const int h = key & (W - 1);
+  const double PI2_OVER_N = 2 * kPi / c.n;
+#pragma unroll
+  for (int l = 0; l < 2; l++) {
+    double s, co;
+    sincos(PI2_OVER_N * key * (double)(c.io + l), &s, &co);
+    const double rr = (double)W * (v.x * co - v.y * s);
+    const double ri = (double)W * (v.x * s + v.y * co);
+    double *p = (double *)&c.man[2 * h + l];
+    atomicAdd(p, -rr);
+    atomicAdd(p + 1, -ri);
+  }
+}
+
+__device__ void update_all(const PeelCtx &c, int key, double2 v, int *err) {
+  const V3Dev &d = *c.d;
+  const int k2 = (int)((((long long)key * c.ai) % c.n + c.shift) % c.n);
+  update_gauss(c, c.g2, (const double2 *)d.win2, d.win2_half, d.B2, k2, v, c.aG, 1, err);
+  update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, key, v, c.ig, 1, err);
+  update_mansour(c, key, v);
+}
+
+// Result map: key -> accumulated value; returns nothing, keys of one round
+// are distinct so the value update has a single writer.
+__device__ void map_add(const PeelCtx &c, int key, double2 v, bool assign, int *count, int cap,
+                        int *err) {
+  unsigned h = ((unsigned)key * 2654435761u) & (unsigned)c.tmask;
+  for (int probe = 0; probe <= c.tmask; probe++) {
+    const int cur = atomicCAS(&c.tkey[h], -1, key);
+    if (cur == -1) {
+      const int idx = atomicAdd(count, 1);
+      if (idx < cap)
+        c.list[idx] = (int)h;
+      else
+        atomicOr(err, ERR_V3_CAP);
+      c.tval[h] = v;
+      return;
+    }
+    if (cur == key) {
+      if (assign) {
+        c.tval[h] = v;
+      } else {
+        double2 o = c.tval[h];
+        c.tval[h] = make_double2(o.x + v.x, o.y + v.y);
+      }
+      return;
+    }
+    h = (h + 1) & (unsigned)c.tmask;
+  }
+  atomicOr(err, ERR_V3_CAP);
+}
+
+// estimate_freq_mansour_loops2 (computefourier-3.0.cc:642-776)
+__device__ void est_mansour(const PeelCtx &c, int *nfound, int cap, int *err) {
+  const int W = c.d->W, n = c.n;
+  const double PI2 = 2 * kPi, N_OVER_PI2 = n / PI2, PI2_OVER_N = PI2 / n;
+  const unsigned FREQ_MASK = ((unsigned)(n - 1) & ~((unsigned)W - 1));
+  const double NORM = 1. / W, NORM2 = NORM * NORM;
+  for (int bk = threadIdx.x; bk < W; bk += blockDim.x) {
+    const double2 s0 = c.man[2 * bk], s1 = c.man[2 * bk + 1];
+    const double c0 = (s0.x * s0.x + s0.y * s0.y) * NORM2;
+    const double c1 = (s1.x * s1.x + s1.y * s1.y) * NORM2;
+    if (!(c0 + c1 > 1e-8)) continue;
+    const double d0 = atan2(s0.y * NORM, s0.x * NORM), d1 = atan2(s1.y * NORM, s1.x * NORM);
+    const double bb = (c1 * (1. / c0)) - 1;
+    if ((bb * bb < n * 1e-10) && (c0 > 0.01)) {
+      const int freq1 = (int)__double2ll_rn((d1 - d0) * N_OVER_PI2);
+      const int freq3 = (int)((unsigned)freq1 & FREQ_MASK) | bk;
+      const double ph = d0 - PI2_OVER_N * wrapmul(freq3, c.io);
+      const double ab = sqrt(c0);
+      double s, co;
+      sincos(ph, &s, &co);
+      const int i = atomicAdd(nfound, 1);
+      if (i < cap) {
+        c.est_f[i] = freq3;
+        c.est_v[i] = make_double2(ab * co, ab * s);
+      } else {
+        atomicOr(err, ERR_V3_CAP);
+      }
+    }
+  }
+}
+
+// estimate_freq_gauss_loops2 (computefourier-3.0.cc:484-640)
+__device__ void est_gauss(const PeelCtx &c, const double2 *SAMP, int B, const double2 *win,
+                          int half, int a, int b, int *nfound, int cap, int *err) {
+  const int n = c.n;
+  const unsigned n1 = n - 1, B1 = B - 1;
+  const double PI2 = 2 * kPi, N_OVER_PI2 = n / PI2;
+  const double PI2_A_OFFSET_OVER_N = PI2 * a * c.ig / n;
+  const double BUCKETS_OVER_N = (double)B / n;
+  const unsigned q = n / B;
+  for (int bk = threadIdx.x; bk < B; bk += blockDim.x) {
+    const double2 s0 = SAMP[2 * bk], s1 = SAMP[2 * bk + 1];
+    const double c0 = s0.x * s0.x + s0.y * s0.y;
+    const double c1 = s1.x * s1.x + s1.y * s1.y;
+    if (!(c0 + c1 > 1e-8)) continue;
+    const double d0 = atan2(s0.y, s0.x), d1 = atan2(s1.y, s1.x);
+    const double eb = c1 / c0 - 1;
+    const double err2 = (eb * eb) / n;
+    if ((err2 < 1e-12) && (c0 > 0.01)) {
+      const int freq = (int)((unsigned)((int)__double2ll_rn(N_OVER_PI2 * (d1 - d0)) + n) & n1);
+      const unsigned hashed = (unsigned)__double2ll_rn(freq * BUCKETS_OVER_N) & B1;
+      if (hashed == (unsigned)bk) {
+        const double ph = d0 - PI2_A_OFFSET_OVER_N * freq;
+        const double r = sqrt(c0);
+        double s, co;
+        sincos(ph, &s, &co);
+        const double mr = r * co, mi = r * s;
+        const int dist = (int)((hashed * q - (unsigned)freq + (unsigned)n) & n1);
+        const double2 f = win_at(win, half, n, dist, err);
+        const double den = f.x * f.x + f.y * f.y;
+        const double2 v = make_double2((mr * f.x + mi * f.y) / den, (mi * f.x - mr * f.y) / den);
+        const int fo = (int)((unsigned)((int)(((long long)freq * a) % n) - b + n) & n1);
+        const int i = atomicAdd(nfound, 1);
+        if (i < cap) {
+          c.est_f[i] = fo;
+          c.est_v[i] = v;
+        } else {
+          atomicOr(err, ERR_V3_CAP);
+        }
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void trace_rec(const V3Dev &d, int slot, int *cnt, int round, int stage, int key,
+                                          double2 v) {
+  if (slot != 0 || !d.trace) return;
+  const int i = atomicAdd(&cnt[CNT_TRACE], 1);
+  if (i < d.trace_cap) {
+    double *t = d.trace + 5 * (long)i;
+    t[0] = round;
+    t[1] = stage;
+    t[2] = key;
+    t[3] = v.x;
+    t[4] = v.y;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_v3_peel(V3Dev d) {
+  __shared__ int s_found, s_count, s_err, s_cnt[3], s_prev[3], s_stop;
+  const int slot = blockIdx.x;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  PeelCtx c;
+  c.d = &d;
+  c.n = d.n;
+  c.n1 = d.n - 1;
+  c.man = (double2 *)d.man + (long)slot * 2 * d.W;
+  c.g1 = (double2 *)d.g1 + (long)slot * 2 * d.B1;
+  c.g2 = (double2 *)d.g2 + (long)slot * 2 * d.B2;
+  c.tkey = d.map_keys + (long)slot * d.table_cap;
+  c.tval = (double2 *)d.map_vals + (long)slot * d.table_cap;
+  c.list = d.map_table + (long)slot * d.map_cap;
+  c.tmask = d.table_cap - 1;
+  c.est_f = d.est_f + (long)slot * d.est_cap;
+  c.est_v = (double2 *)d.est_v + (long)slot * d.est_cap;
+  c.a = rp[0];
+  c.ai = rp[1];
+  c.b = rp[2];
+  c.io = rp[3];
+  c.ig = rp[4];
+  c.aG = wrapmul(c.a, c.ig);
+  c.shift = ((wrapmul(c.ai, c.b) % d.n) + d.n) % d.n;
+  int *cnt = d.counters + slot * CNT_STRIDE;
+  const int T = blockDim.x;
+  if (threadIdx.x == 0) {
+    s_found = 0;
+    s_count = 0;
+    s_err = 0;
+    s_stop = 0;
+    for (int i = 0; i < 3; i++) s_prev[i] = 0;
+  }
+  __syncthreads();
+
+  // ---- Mansour estimate; first tones are assigned, their buckets cleared
+  est_mansour(c, &s_found, d.est_cap, &s_err);
+  __syncthreads();
+  int F = min(s_found, d.est_cap);
+  for (int i = threadIdx.x; i < F; i += T) {
+    trace_rec(d, slot, cnt, -2, 0, c.est_f[i], c.est_v[i]);
+    map_add(c, c.est_f[i], c.est_v[i], true, &s_count, d.map_cap, &s_err);
+    const int bk = c.est_f[i] % d.W;
+    c.man[2 * bk] = make_double2(0.0, 0.0);
+    c.man[2 * bk + 1] = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  if (F == d.k) {  // the reference returns before writing its output (:859-860)
+    if (threadIdx.x == 0) {
+      cnt[CNT_OUT] = 0;
+      cnt[CNT_V3] = -1;
+    }
+    return;
+  }
+
+  // ---- first Gaussian filter: peel the known tones, estimate, peel
+  int M = min(s_count, d.map_cap);
+  for (int i = threadIdx.x; i < M; i += T) {
+    const int h = c.list[i];
+    update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, c.tkey[h], c.tval[h], c.ig, 1,
+                 &s_err);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_found = 0;
+  __syncthreads();
+  est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &s_found, d.est_cap, &s_err);
+  __syncthreads();
+  F = min(s_found, d.est_cap);
+  for (int i = threadIdx.x; i < F; i += T) {
+    trace_rec(d, slot, cnt, -1, 1, c.est_f[i], c.est_v[i]);
+    map_add(c, c.est_f[i], c.est_v[i], false, &s_count, d.map_cap, &s_err);
+    update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, c.est_f[i], c.est_v[i], c.ig, 1,
+                 &s_err);
+    update_mansour(c, c.est_f[i], c.est_v[i]);
+  }
+  __syncthreads();
+
+  // ---- second (permuted) Gaussian filter: peel every known tone
+  M = min(s_count, d.map_cap);
+  for (int i = threadIdx.x; i < M; i += T) {
+    const int h = c.list[i];
+    const int key = c.tkey[h];
+    const int k2 = (int)((((long long)key * c.ai) % d.n + c.shift) % d.n);
+    update_gauss(c, c.g2, (const double2 *)d.win2, d.win2_half, d.B2, k2, c.tval[h], c.aG, 1, &s_err);
+  }
+  __syncthreads();
+
+  // ---- round robin: G2, then Mansour, G1, G2, ... until the counts of
+  //      non-empty buckets repeat after a G2 round (:959-1076)
+  int stage = 2, rounds = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_found = 0;
+    __syncthreads();
+    if (stage == 0)
+      est_mansour(c, &s_found, d.est_cap, &s_err);
+    else if (stage == 1)
+      est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &s_found, d.est_cap, &s_err);
+    else
+      est_gauss(c, c.g2, d.B2, (const double2 *)d.win2, d.win2_half, c.a, c.b, &s_found, d.est_cap,
+                &s_err);
+    __syncthreads();
+    F = min(s_found, d.est_cap);
+    for (int i = threadIdx.x; i < F; i += T) {
+      trace_rec(d, slot, cnt, rounds, stage, c.est_f[i], c.est_v[i]);
+      map_add(c, c.est_f[i], c.est_v[i], false, &s_count, d.map_cap, &s_err);
+      update_all(c, c.est_f[i], c.est_v[i], &s_err);
+    }
+    __syncthreads();
+    if (stage == 2 && rounds >= 1) {
+      if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
+      __syncthreads();
+      int cm = 0, c1 = 0, c2 = 0;
+      for (int j = threadIdx.x; j < d.B1; j += T) {
+        const double2 v = c.g1[j];
+        c1 += (v.x * v.x + v.y * v.y > 1e-6);
+      }
+      for (int j = threadIdx.x; j < d.B2; j += T) {
+        const double2 v = c.g2[j];
+        c2 += (v.x * v.x + v.y * v.y > 1e-6);
+      }
+      for (int j = threadIdx.x; j < d.W; j += T) {
+        const double2 v = c.man[2 * j];
+        const double re = v.x / d.W, im = v.y / d.W;
+        cm += (re * re + im * im > 1e-6);
+      }
+      atomicAdd(&s_cnt[0], cm);
+      atomicAdd(&s_cnt[1], c1);
+      atomicAdd(&s_cnt[2], c2);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        s_stop = (s_cnt[0] == s_prev[0] && s_cnt[1] == s_prev[1] && s_cnt[2] == s_prev[2]);
+        for (int i = 0; i < 3; i++) s_prev[i] = s_cnt[i];
+      }
+      __syncthreads();
+      if (s_stop) break;
+    }
+    rounds++;
+    if (rounds > d.max_passes) {
+      if (threadIdx.x == 0) s_err |= ERR_V3_NOCONVERGE;
+      break;
+    }
+    stage = (stage + 1) % 3;
+  }
+  __syncthreads();
+
+  // ---- output: every key of the map with its accumulated value
+  M = min(s_count, d.map_cap);
+  const int outn = min(M, d.out_cap);
+  for (int i = threadIdx.x; i < outn; i += T) {
+    const int h = c.list[i];
+    d.out_idx[(long)slot * d.out_cap + i] = c.tkey[h];
+    ((double2 *)d.out_val)[(long)slot * d.out_cap + i] = c.tval[h];
+  }
+  if (threadIdx.x == 0) {
+    cnt[CNT_OUT] = outn;
+    cnt[CNT_V3] = rounds;
+    cnt[CNT_ERR] |= s_err | (M > d.out_cap ? ERR_OUT_OVERFLOW : 0);
+  }
+}
+
+// ---------------------------------------------------------------- launch --
+
+cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t s, StageEvents *se) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(d.counters, 0, sizeof(int) * CNT_STRIDE * nslots, s))) return e;
+  if ((e = cudaMemsetAsync(d.map_keys, 0xFF, sizeof(int) * (size_t)d.table_cap * nslots, s))) return e;
+  int Nmax = d.W;
+  if (d.B1 > Nmax) Nmax = d.B1;
+  if (d.B2 > Nmax) Nmax = d.B2;
+  int T = Nmax / 4;
+  if (T > 1024) T = 1024;
+  if (T < 32) T = 32;
+  const int per = (Nmax / 4 + T - 1) / T;
+  const size_t sm = (size_t)Nmax * sizeof(double2);
+  dim3 grid(6, nslots);
+  mark(se, s);
+  switch (per) {
+    case 1:
+      if (sm > 48 * 1024 &&
+          (e = cudaFuncSetAttribute(k_v3_filters<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)))
+        return e;
+      k_v3_filters<1><<<grid, T, sm, s>>>(d);
+      break;
+    case 2:
+      if (sm > 48 * 1024 &&
+          (e = cudaFuncSetAttribute(k_v3_filters<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)))
+        return e;
+      k_v3_filters<2><<<grid, T, sm, s>>>(d);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  if ((e = cudaGetLastError())) return e;
+  mark(se, s);
+  k_v3_peel<<<nslots, 1024, 0, s>>>(d);
+  mark(se, s);
+  note_launches(2);
+  return cudaGetLastError();
+}
+
+}  // namespace sfft

@@ -1,0 +1,75 @@
+"""Host-side checks of the C-ABI library that need no GPU: it builds, loads,
+exports every function include/sfft.h declares, fails loudly without a
+device, and computes plans identical to the reference's (via the oracle)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from sfft_gb300 import _lib, build
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = _lib.header_functions()
+    for required in ("sfft_malloc", "sfft_free", "sfft_make_plan", "sfft_free_plan", "sfft_exec",
+                     "sfft_exec_many"):
+        assert required in names
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_plan_struct_layout_matches_reference():
+    # src/sfft.h:44-50: {sfft_version version; unsigned n, k; void *data;}
+    assert ctypes.sizeof(_lib.Plan) == 24
+    assert _lib.Plan.data.offset == 16
+
+
+def test_malloc_is_aligned_and_freeable(lib):
+    p = lib.sfft_malloc(1 << 20)
+    assert p and p % 16 == 0
+    lib.sfft_free(p)
+    lib.sfft_free(None)
+
+
+def test_no_device_means_no_plan(lib):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    plan = lib.sfft_make_plan(1 << 16, 50, 0, _lib.FFTW_ESTIMATE)
+    assert not plan
+    assert "CUDA" in _lib.last_error()
+
+
+def test_invalid_arguments_rejected(lib):
+    assert not lib.sfft_make_plan(1000, 50, 0, _lib.FFTW_ESTIMATE)        # not a power of two
+    assert _lib.last_error()
+    assert not lib.sfft_make_plan(1 << 16, 50, 7, _lib.FFTW_ESTIMATE)     # no such version
+    f = (ctypes.c_long * 11)()
+    assert lib.sfft_describe_plan(1 << 14, 4, 2, f, 11) == -1              # v3 needs k >= 8
+    assert lib.sfft_describe_plan(8192, 1000, 0, f, 11) == -1              # B < 2k+1
+
+
+PLAN_CASES = [(8192, 50, 1), (1 << 16, 50, 1), (1 << 16, 50, 2), (1 << 18, 100, 2), (1 << 20, 50, 2),
+              (1 << 16, 50, 3), (1 << 18, 100, 3), (1 << 14, 8, 3), (4000, 100, 1)]
+
+
+@pytest.mark.parametrize("n,k,v", [c for c in PLAN_CASES if c[0] & (c[0] - 1) == 0])
+def test_plans_identical_to_oracle(lib, oracle_lib, n, k, v):
+    from sfft_gb300 import sfft as S
+    op = oracle_lib.OraclePlan(n, k, v - 1)
+    mine = S.describe_plan(n, k, v)
+    for key, val in mine.items():
+        assert op.params[key] == val, key
+    for which in (0, 1):
+        t, f = S.describe_filter(n, k, v, which)
+        np.testing.assert_array_equal(t, op.filter_time(which))
+        np.testing.assert_array_equal(f, op.filter_freq(which))
