@@ -154,6 +154,24 @@ long sfft_profile_read(sfft_plan *plan, double *stage_ms, int nstage);
 /* Number of GPU kernels this library has launched in this process. */
 long sfft_kernel_launches(void);
 
+/* sfft_exec_noalloc has no counterpart in the reference.  One v1/v2
+ * transform that allocates no GPU memory, for callers that cannot call
+ * cudaMalloc while they run (memory handed to their own pool, a fixed
+ * budget after start-up, or a latency-bound stream that must not be
+ * synchronised by cudaMalloc/cudaFree).  Its scratch is a static 3 MiB
+ * device array in this library (held on every GPU that loads it), so plans
+ * are limited to n <= 2^18, at most 65536 bucket samples and 32 loops;
+ * larger plans return -1.  d_in: device signal of type in_type; outputs:
+ * device buffers of at least sfft_output_capacity(plan) entries
+ * (complex128 values for FP64 plans, complex64 for FP32 plans);
+ * d_status: device int[2] receiving the coefficient count and the device
+ * error bits.  Asynchronous on `stream` (a cudaStream_t).  The first call
+ * on a device looks up the static array and should precede any stream
+ * capture; all calls share the array, so calls whose GPU work overlaps
+ * race.  Returns 0, or -1 with sfft_last_error() set. */
+long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type, int *d_out_idx, void *d_out_val,
+                       long cap, int *d_status, void *stream);
+
 /* Host-only plan queries (no GPU needed): the parameters a plan for
  * (n, k, version) would use, as the reference computes them.  fields:
  * v1/v2: B_loc, B_thresh, B_est, W_Comb, Comb_loops, loops_loc,

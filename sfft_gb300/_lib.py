@@ -81,6 +81,8 @@ def load(build_if_missing=False):
     L.sfft_profile.argtypes = [PP, ci]
     L.sfft_profile_read.restype = cl
     L.sfft_profile_read.argtypes = [PP, ctypes.POINTER(ctypes.c_double), ci]
+    L.sfft_exec_noalloc.restype = cl
+    L.sfft_exec_noalloc.argtypes = [PP, vp, ci, vp, vp, cl, vp, vp]
     L.sfft_kernel_launches.restype = cl
     L.sfft_kernel_launches.argtypes = []
     _lib = L

@@ -20,7 +20,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsfft.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["v12.cu", "v3.cu"]
+CU_SOURCES = ["v12.cu", "v3.cu", "noalloc.cu"]
 # v3 reproduces the reference's phase arguments (up to ~1e12 rad), whose
 # last-ulp rounding matters: no multiply-add contraction in that file.
 CU_EXTRA = {"v3.cu": ["--fmad=false"]}

@@ -529,6 +529,29 @@ bool exec_dense_chunk(PlanImpl &P, int num, complex_t **in, complex_t **out) {
 
 }  // namespace
 
+namespace sfft {
+
+// For entry points that bring their own workspace: the plan's constants
+// and sizes (workspace pointers of the view are the plan's and must be
+// replaced by the caller).  Returns false for plans other than v1/v2.
+bool plan_v12_constants(sfft_plan *plan, V12Dev *d, int *hit_cap, int *out_cap) {
+  PlanImpl *P = impl(plan);
+  if (!P || P->version > 1) return false;
+  *d = v12_view(*P);
+  *hit_cap = P->hit_cap;
+  *out_cap = P->out_cap;
+  return true;
+}
+
+// The random draws of one transform, in the reference's order.
+void plan_draw(sfft_plan *plan, int *rp, unsigned epoch) { draw_params(*impl(plan), rp, epoch); }
+
+int plan_device(sfft_plan *plan) { return impl(plan)->device; }
+
+void set_last_error(const char *m) { set_err(m); }
+
+}  // namespace sfft
+
 // =================================================================== C API
 
 extern "C" {
