@@ -158,7 +158,7 @@ long sfft_kernel_launches(void);
  * transform that allocates no GPU memory, for callers that cannot call
  * cudaMalloc while they run (memory handed to their own pool, a fixed
  * budget after start-up, or a latency-bound stream that must not be
- * synchronised by cudaMalloc/cudaFree).  Its scratch is a static 3 MiB
+ * synchronised by cudaMalloc/cudaFree).  Its scratch is a static 4 MiB
  * device array in this library (held on every GPU that loads it), so plans
  * are limited to n <= 2^18, at most 65536 bucket samples and 32 loops;
  * larger plans return -1.  d_in: device signal of type in_type; outputs:

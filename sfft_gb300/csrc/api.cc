@@ -120,15 +120,16 @@ struct PlanImpl {
   cudaEvent_t done = nullptr;
   std::mutex mu;
   // constants
-  DBuf taps_a, taps_b, win_a, win_b, tw_a, tw_b, tw_c;
+  DBuf taps_a, taps_b, win_a, win_b, win32_a, win32_b, tw_a, tw_b, tw_c;
   int win_half_a = 0, win_half_b = 0;
   // workspace
   int slots = 0;
-  DBuf xs, J, score, hits, comb_bits, comb_list, counters, out_idx, out_val;
+  DBuf xs, xs32, xs_tmp, comb_buf, comb_tmp, J, score, hits, comb_bits, comb_list, counters, out_idx, out_val;
   DBuf man, g1, g2, perm, est_f, est_v, map_keys, map_vals, map_list;
   DBuf rparams, inputs, dense_ptrs, in_stage, dense_stage, trace;
   std::vector<unsigned> epoch;
   int hit_cap = 0, out_cap = 0, est_cap = 0, map_cap = 0, table_cap = 0;
+  int large_b = 0, large_c = 0;  // FFTs longer than one CTA's shared memory
   int rp_stride = 0;
   std::vector<int> last_rp;  // draws of the last exec (slot 0)
   // stage timing (sfft_profile): event sets of launches not yet harvested
@@ -249,6 +250,11 @@ bool ensure_slots(PlanImpl &P, int want) {
                     : 1;
     const long comb_max = std::min<long>((long)p.W_Comb, (long)p.Comb_loops * p.B_thresh);
     P.out_cap = P.version == 0 ? P.hit_cap : (int)(comb_max * (P.n / p.W_Comb));
+    if (P.prec == sfft::PREC_FP64 && !P.xs32.ensure(8 * p.x_samp_size * S)) return false;
+    if (P.large_b && !P.xs_tmp.ensure(cs * p.x_samp_size * S)) return false;
+    if (P.large_c && (!P.comb_buf.ensure(cs * (size_t)p.Comb_loops * p.W_Comb * S) ||
+                      !P.comb_tmp.ensure(cs * (size_t)p.Comb_loops * p.W_Comb * S)))
+      return false;
     if (!P.xs.ensure(cs * p.x_samp_size * S) || !P.J.ensure(sizeof(int) * L * p.B_thresh * S) ||
         !P.hits.ensure(sizeof(int) * P.hit_cap * S) ||
         !P.comb_bits.ensure(sizeof(unsigned) * ((p.W_Comb + 31) / 32) * S) ||
@@ -270,6 +276,7 @@ bool ensure_slots(PlanImpl &P, int want) {
     P.table_cap = 1;
     while (P.table_cap < 2 * P.map_cap) P.table_cap <<= 1;
     P.out_cap = P.map_cap;
+    if (!P.perm.ensure(16 * 2 * (size_t)(p.w_g2 + 2) * S)) return false;
     if (!P.man.ensure(32 * (size_t)p.W_Man * S) || !P.g1.ensure(32 * (size_t)p.B_g1 * S) ||
         !P.g2.ensure(32 * (size_t)p.B_g2 * S) || !P.est_f.ensure(sizeof(int) * P.est_cap * S) ||
         !P.est_v.ensure(16 * (size_t)P.est_cap * S) || !P.map_keys.ensure(sizeof(int) * P.table_cap * S) ||
@@ -348,6 +355,14 @@ sfft::V12Dev v12_view(PlanImpl &P) {
   d.tw_est = P.tw_b.p;
   d.tw_comb = P.tw_c.p;
   d.xs = P.xs.p;
+  d.xs32 = P.prec == sfft::PREC_FP64 ? P.xs32.p : nullptr;
+  d.xs_tmp = P.xs_tmp.p;
+  d.comb_buf = P.comb_buf.p;
+  d.comb_tmp = P.comb_tmp.p;
+  d.large_buckets = P.large_b;
+  d.large_comb = P.large_c;
+  d.win32_loc = P.win32_a.p;
+  d.win32_est = P.win32_b.p;
   d.J = P.J.as<int>();
   d.score = P.score.as<unsigned>();
   d.hits = P.hits.as<int>();
@@ -627,9 +642,17 @@ sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_o
       return nullptr;
     }
     const auto &p = P->p12;
-    const int mx = sfft::v12_max_fft(P->prec);
-    if (p.B_loc > mx || p.B_est > mx || (P->version == 1 && p.W_Comb > mx)) {
-      set_err("bucket FFT longer than " + std::to_string(mx) + " points is not supported by this build");
+    int mx = sfft::v12_max_fft(P->prec);
+    // SFFT_GB300_MAX_SMEM_FFT lowers the shared-memory FFT limit so the
+    // global-memory path can be exercised at small sizes
+    if (const char *ov = std::getenv("SFFT_GB300_MAX_SMEM_FFT")) {
+      const int v = std::atoi(ov);
+      if (v >= 16 && v < mx) mx = v;
+    }
+    P->large_b = (p.B_loc > mx || p.B_est > mx);
+    P->large_c = (P->version == 1 && p.W_Comb > mx);
+    if (p.B_loc > (1 << 20) || p.B_est > (1 << 20) || p.W_Comb > (1 << 22)) {
+      set_err("bucket or comb FFT longer than 2^20 points");
       return nullptr;
     }
     if (L12(*P) > 32) {
@@ -639,6 +662,9 @@ sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_o
     if (!upload_taps(P->taps_a, fa.time, P->prec) || !upload_taps(P->taps_b, fb.time, P->prec) ||
         !upload_v12_window(P->win_a, fa.freq, n, n / p.B_loc, P->prec) ||
         !upload_v12_window(P->win_b, fb.freq, n, n / p.B_est, P->prec) ||
+        (P->prec == sfft::PREC_FP64 &&
+         (!upload_v12_window(P->win32_a, fa.freq, n, n / p.B_loc, sfft::PREC_FP32) ||
+          !upload_v12_window(P->win32_b, fb.freq, n, n / p.B_est, sfft::PREC_FP32))) ||
         !upload_twiddles(P->tw_a, p.B_loc, P->prec) || !upload_twiddles(P->tw_b, p.B_est, P->prec) ||
         !upload_twiddles(P->tw_c, std::max(p.W_Comb, 2), P->prec))
       return nullptr;

@@ -196,9 +196,9 @@ __device__ void block_fft(c2_t<R> *buf, int N, int logN, const c2_t<R> *__restri
 // equal to it in increasing order until num; the output is ascending.
 // keys: order-preserving keys of p in shared memory.  hist: 256 + 2 ints of
 // shared memory; scan: 64 ints.  Writes out[0..num).  Block-wide.
-template <typename K>
-__device__ void block_top_indices(const K *keys, int N, int num, int *__restrict__ out,
-                                  int *hist, int *scan) {
+template <typename K, typename KeyAt>
+__device__ void block_top_indices_f(KeyAt keyat, int N, int num, int *__restrict__ out, int *hist,
+                                    int *scan) {
   constexpr int BITS = sizeof(K) * 8;
   const int rank = N - num - 1;  // ascending rank of the cutoff
   K prefix = 0, mask = 0;
@@ -207,7 +207,7 @@ __device__ void block_top_indices(const K *keys, int N, int num, int *__restrict
     for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      K k = keys[i];
+      K k = keyat(i);
       if ((k & mask) == prefix) atomicAdd(&hist[(int)((k >> shift) & 0xFF)], 1);
     }
     __syncthreads();
@@ -249,7 +249,7 @@ __device__ void block_top_indices(const K *keys, int N, int num, int *__restrict
   const int lo = min(N, (int)threadIdx.x * C), hi = min(N, lo + C);
   int ngt = 0, neq = 0;
   for (int i = lo; i < hi; i++) {
-    K k = keys[i];
+    K k = keyat(i);
     ngt += (k > cutoff);
     neq += (k == cutoff);
   }
@@ -259,7 +259,7 @@ __device__ void block_top_indices(const K *keys, int N, int num, int *__restrict
   int pos = pgt + min(peq, max(need, 0));
   int eqr = peq;
   for (int i = lo; i < hi; i++) {
-    K k = keys[i];
+    K k = keyat(i);
     if (k > cutoff) {
       if (pos < num) out[pos] = i;
       pos++;
@@ -272,6 +272,48 @@ __device__ void block_top_indices(const K *keys, int N, int num, int *__restrict
     }
   }
   __syncthreads();
+}
+
+template <typename K>
+__device__ void block_top_indices(const K *keys, int N, int num, int *__restrict__ out, int *hist,
+                                  int *scan) {
+  block_top_indices_f<K>([keys](int i) { return keys[i]; }, N, num, out, hist, scan);
+}
+
+// One radix-R stage (R = 2 with Ns = 1, or R = 4) of block_fft's Stockham
+// FFT on arrays in global memory: butterfly j of array `arr`.  Same
+// operations, same order, same rounding as the shared-memory stages.
+template <typename R>
+__device__ __forceinline__ void stockham_stage(const c2_t<R> *__restrict__ src, c2_t<R> *__restrict__ dst,
+                                               int N, int Ns, int radix, int j,
+                                               const c2_t<R> *__restrict__ tw) {
+  using V = c2_t<R>;
+  if (radix == 2) {
+    const int h = N >> 1;
+    const V a = src[j], b = src[j + h];
+    dst[2 * j] = cadd<R>(a, b);
+    dst[2 * j + 1] = csub<R>(a, b);
+    return;
+  }
+  const int q4 = N >> 2, stride = N / (Ns * 4), k = j & (Ns - 1);
+  V v[4];
+#pragma unroll
+  for (int r = 0; r < 4; r++) v[r] = src[j + r * q4];
+#pragma unroll
+  for (int r = 1; r < 4; r++) {
+    const int e = r * k * stride;
+    if (e) v[r] = cmul<R>(v[r], tw[e]);
+  }
+  const V t0 = cadd<R>(v[0], v[2]), t1 = csub<R>(v[0], v[2]);
+  const V t2 = cadd<R>(v[1], v[3]), t3 = csub<R>(v[1], v[3]);
+  V u3;
+  u3.x = t3.y;
+  u3.y = -t3.x;
+  const int base = (j - k) * 4 + k;
+  dst[base] = cadd<R>(t0, t2);
+  dst[base + Ns] = cadd<R>(t1, u3);
+  dst[base + 2 * Ns] = csub<R>(t0, t2);
+  dst[base + 3 * Ns] = csub<R>(t1, u3);
 }
 
 }  // namespace sfft

@@ -42,8 +42,13 @@ struct V12Dev {
   const void *taps_loc, *taps_est;  // w complex (double2 or float2)
   const void *win_loc, *win_est;    // q entries: FP64 double4 (c, d, c^2+d^2, 0); FP32 float2 (g)
   const void *tw_loc, *tw_est, *tw_comb;  // twiddle tables (double2 or float2)
+  const void *win32_loc, *win32_est;  // FP64 plans: float2 g = conj-scaled window for bounds
   // per-slot workspace
   void *xs;                 // xs_size complex per slot
+  void *xs32;               // FP64 plans: float2 copy of xs (median pre-selection)
+  void *xs_tmp;             // large bucket FFTs: ping-pong partner of xs
+  void *comb_buf, *comb_tmp;  // large comb FFTs: comb_loops * W per slot
+  int large_buckets, large_comb;  // FFT longer than one CTA's shared memory
   int *J;                   // L * num per slot
   unsigned *score;          // n per slot: (epoch << 8) | votes
   int *hits;                // hit_cap per slot

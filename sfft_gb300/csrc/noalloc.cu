@@ -12,7 +12,7 @@
 // (filter taps, estimation windows, twiddle tables) were placed on the
 // device when the plan was made and are only read here.
 //
-// Limits: the array holds SFFT_NOALLOC_SCRATCH_BYTES (3 MiB) on every GPU
+// Limits: the array holds SFFT_NOALLOC_SCRATCH_BYTES (4 MiB) on every GPU
 // that loads the library, for the life of the process.  That covers v1/v2
 // plans with n <= 2^18, at most 65536 bucket samples and at most 32 loops;
 // larger plans are rejected with an error.
@@ -41,7 +41,7 @@ int plan_device(sfft_plan *plan);
 void set_last_error(const char *m);
 }  // namespace sfft
 
-#define SFFT_NOALLOC_SCRATCH_BYTES (3u << 20)
+#define SFFT_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define SFFT_NOALLOC_MAX_N (1 << 18)
 #define SFFT_NOALLOC_MAX_XS 65536L
 #define SFFT_NOALLOC_MAX_LOOPS 32
@@ -89,6 +89,8 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
   off += up256(sizeof(void *));
   const size_t o_xs = off;
   off += up256(cs * (size_t)d.xs_size);
+  const size_t o_xs32 = off;
+  if (d.prec == PREC_FP64) off += up256(8 * (size_t)d.xs_size);
   const size_t o_J = off;
   off += up256(sizeof(int) * (size_t)L * d.num);
   const size_t o_score = off;
@@ -99,9 +101,9 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
   off += up256(sizeof(unsigned) * (size_t)((d.W + 31) / 32));
   const size_t o_list = off;
   off += up256(sizeof(int) * (size_t)d.W);
-  if (d.n > SFFT_NOALLOC_MAX_N || d.xs_size > SFFT_NOALLOC_MAX_XS || L > SFFT_NOALLOC_MAX_LOOPS ||
+  if (d.large_buckets || d.large_comb || d.n > SFFT_NOALLOC_MAX_N || d.xs_size > SFFT_NOALLOC_MAX_XS || L > SFFT_NOALLOC_MAX_LOOPS ||
       off > SFFT_NOALLOC_SCRATCH_BYTES) {
-    set_last_error("sfft_exec_noalloc: plan exceeds the 3 MiB static scratch (limits: n <= 2^18, "
+    set_last_error("sfft_exec_noalloc: plan exceeds the 4 MiB static scratch (limits: n <= 2^18, "
                    "at most 65536 bucket samples, at most 32 loops)");
     return -1;
   }
@@ -149,6 +151,7 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
   // the vote counters of other plans' calls carry other tags: stale
   // entries read as zero; they must cover this plan's n, which the layout ensures
   d.xs = base + o_xs;
+  d.xs32 = d.prec == PREC_FP64 ? base + o_xs32 : nullptr;
   d.J = (int *)(base + o_J);
   d.score = (unsigned *)(base + o_score);
   d.hits = (int *)(base + o_hits);

@@ -141,36 +141,12 @@ __global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) {
   if (threadIdx.x == 0) d.counters[slot * CNT_STRIDE + CNT_COMB] = tot.x;
 }
 
-// ---------------------------------------------------------------- bucket --
-
-template <typename R, int PER>
-__global__ void __launch_bounds__(1024) k_bucket(V12Dev d) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int j = blockIdx.x, slot = blockIdx.y;
-  const bool loc = j < d.L_loc;
-  const int B = loc ? d.B_loc : d.B_est;
-  const long off = loc ? (long)j * d.B_loc : (long)d.L_loc * d.B_loc + (long)(j - d.L_loc) * d.B_est;
-  c2_t<R> *buf;
-  key_t<R> *keys;
-  int *hist, *scan, *Js;
-  carve<R>(smem, B, buf, keys, hist, scan, Js);
-  c2_t<R> *xs = (c2_t<R> *)d.xs + (long)slot * d.xs_size + off;
-  for (int i = threadIdx.x; i < B; i += blockDim.x) buf[i] = xs[i];
-  __syncthreads();
-  block_fft<R, PER>(buf, B, dlog2(B), (const c2_t<R> *)(loc ? d.tw_loc : d.tw_est));
-  for (int i = threadIdx.x; i < B; i += blockDim.x) {
-    const c2_t<R> v = buf[i];
-    xs[i] = v;
-    keys[i] = pkey(cabs2<R>(v));
-  }
-  __syncthreads();
-  block_top_indices<key_t<R>>(keys, B, d.num, Js, hist, scan);
-  int *Jg = d.J + ((long)slot * d.L + j) * d.num;
-  for (int i = threadIdx.x; i < d.num; i += blockDim.x) Jg[i] = Js[i];
-  if (!loc) return;
-
-  // voting: positions p in [J*q - floor(q/2), +q) (mod n) map to
-  // frequencies f = p * a (mod n)   (computefourier-1.0-2.0.cc:99-113, :147-181)
+// Voting of location loop j: positions p in [J*q - floor(q/2), +q) (mod n)
+// map to frequencies f = p * a (mod n); each gets one vote (v2: only if
+// f mod W is a comb residue); reaching the threshold appends f to the
+// hits (computefourier-1.0-2.0.cc:91-116, :125-184).  Counters carry the
+// exec's epoch in their upper 24 bits, so they never need clearing.
+__device__ void vote_loop(const V12Dev &d, int slot, int j, const int *Js) {
   const int *rp = d.rparams + (long)slot * d.rp_stride;
   const unsigned long long a = (unsigned)rp[j];
   const unsigned ep = (unsigned)rp[2 * d.L + d.comb_loops];
@@ -210,74 +186,311 @@ __global__ void __launch_bounds__(1024) k_bucket(V12Dev d) {
   }
 }
 
+// ---------------------------------------------------------------- bucket --
+
+template <typename R, int PER>
+__global__ void __launch_bounds__(1024) k_bucket(V12Dev d) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int j = blockIdx.x, slot = blockIdx.y;
+  const bool loc = j < d.L_loc;
+  const int B = loc ? d.B_loc : d.B_est;
+  const long off = loc ? (long)j * d.B_loc : (long)d.L_loc * d.B_loc + (long)(j - d.L_loc) * d.B_est;
+  c2_t<R> *buf;
+  key_t<R> *keys;
+  int *hist, *scan, *Js;
+  carve<R>(smem, B, buf, keys, hist, scan, Js);
+  c2_t<R> *xs = (c2_t<R> *)d.xs + (long)slot * d.xs_size + off;
+  for (int i = threadIdx.x; i < B; i += blockDim.x) buf[i] = xs[i];
+  __syncthreads();
+  block_fft<R, PER>(buf, B, dlog2(B), (const c2_t<R> *)(loc ? d.tw_loc : d.tw_est));
+  float2 *xs32 = d.xs32 ? (float2 *)d.xs32 + (long)slot * d.xs_size + off : nullptr;
+  for (int i = threadIdx.x; i < B; i += blockDim.x) {
+    const c2_t<R> v = buf[i];
+    xs[i] = v;
+    if (xs32) xs32[i] = make_float2((float)v.x, (float)v.y);
+    keys[i] = pkey(cabs2<R>(v));
+  }
+  __syncthreads();
+  block_top_indices<key_t<R>>(keys, B, d.num, Js, hist, scan);
+  int *Jg = d.J + ((long)slot * d.L + j) * d.num;
+  for (int i = threadIdx.x; i < d.num; i += blockDim.x) Jg[i] = Js[i];
+  if (loc) vote_loop(d, slot, j, Js);
+}
+
+// ------------------------------------------------- FFTs beyond one CTA --
+
+// One Stockham stage over `narr` arrays of N points per slot.
+template <typename R>
+__global__ void __launch_bounds__(256) k_fft_stage(const c2_t<R> *src, c2_t<R> *dst, int N, int Ns, int radix,
+                                                   long arr_stride, int narr, long slot_stride,
+                                                   const c2_t<R> *tw) {
+  const int slot = blockIdx.y;
+  const int per = N / radix;
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (long)narr * per) return;
+  const int arr = (int)(g / per), j = (int)(g - (long)arr * per);
+  const long base = (long)slot * slot_stride + (long)arr * arr_stride;
+  stockham_stage<R>(src + base, dst + base, N, Ns, radix, j, tw);
+}
+
+// Power, top-2k selection and voting of loop j after a global-memory FFT.
+template <typename R>
+__global__ void __launch_bounds__(1024) k_select_vote(V12Dev d) {
+  __shared__ int hist[264], scan[64];
+  extern __shared__ int Js[];
+  const int j = blockIdx.x, slot = blockIdx.y;
+  const bool loc = j < d.L_loc;
+  const int B = loc ? d.B_loc : d.B_est;
+  const long off = loc ? (long)j * d.B_loc : (long)d.L_loc * d.B_loc + (long)(j - d.L_loc) * d.B_est;
+  const c2_t<R> *xs = (const c2_t<R> *)d.xs + (long)slot * d.xs_size + off;
+  if (d.xs32) {
+    float2 *xs32 = (float2 *)d.xs32 + (long)slot * d.xs_size + off;
+    for (int i = threadIdx.x; i < B; i += blockDim.x) xs32[i] = make_float2((float)xs[i].x, (float)xs[i].y);
+  }
+  block_top_indices_f<key_t<R>>([xs](int i) { return pkey(cabs2<R>(xs[i])); }, B, d.num, Js, hist, scan);
+  int *Jg = d.J + ((long)slot * d.L + j) * d.num;
+  for (int i = threadIdx.x; i < d.num; i += blockDim.x) Jg[i] = Js[i];
+  if (loc) vote_loop(d, slot, j, Js);
+}
+
+template <typename R, typename In>
+__global__ void __launch_bounds__(256) k_comb_gather(V12Dev d) {
+  const int slot = blockIdx.z, c = blockIdx.y, W = d.W;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= W) return;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const long sigma = d.n / W, offset = rp[2 * d.L + c];
+  const In *x = (const In *)d.inputs[slot];
+  ((c2_t<R> *)d.comb_buf)[((long)slot * d.comb_loops + c) * W + i] = cvt_in<R>(__ldg(x + offset + i * sigma));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(1024) k_comb_select(V12Dev d) {
+  __shared__ int hist[264], scan[64];
+  extern __shared__ int Js[];
+  const int c = blockIdx.x, slot = blockIdx.y, W = d.W;
+  const c2_t<R> *v = (const c2_t<R> *)d.comb_buf + ((long)slot * d.comb_loops + c) * W;
+  block_top_indices_f<key_t<R>>([v](int i) { return pkey(cabs2<R>(v[i])); }, W, d.num, Js, hist, scan);
+  unsigned *bits = d.comb_bits + (long)slot * ((W + 31) >> 5);
+  for (int i = threadIdx.x; i < d.num; i += blockDim.x) atomicOr(&bits[Js[i] >> 5], 1u << (Js[i] & 31));
+}
+
+// FFT of `narr` arrays per slot held at a (ping) with b as scratch; the
+// result ends in a.  Stage sequence of block_fft.
+template <typename R>
+static cudaError_t global_fft(c2_t<R> *a, c2_t<R> *b, int N, int narr, long arr_stride, long slot_stride,
+                              int nslots, const c2_t<R> *tw, cudaStream_t s) {
+  int logN = 0;
+  while ((1 << logN) < N) logN++;
+  c2_t<R> *src = a, *dst = b;
+  int Ns = 1, launches = 0;
+  auto stage = [&](int radix) -> cudaError_t {
+    const long work = (long)narr * (N / radix);
+    dim3 grid((unsigned)((work + 255) / 256), nslots);
+    k_fft_stage<R><<<grid, 256, 0, s>>>(src, dst, N, Ns, radix, arr_stride, narr, slot_stride, tw);
+    launches++;
+    c2_t<R> *t = src;
+    src = dst;
+    dst = t;
+    return cudaGetLastError();
+  };
+  cudaError_t e;
+  if (logN & 1) {
+    if ((e = stage(2))) return e;
+    Ns = 2;
+  }
+  while (Ns < N) {
+    if ((e = stage(4))) return e;
+    Ns *= 4;
+  }
+  note_launches(launches);
+  if (src != a) {  // odd number of stages: bring the result home
+    for (int sl = 0; sl < nslots; sl++) {
+      if ((e = cudaMemcpyAsync(a + sl * slot_stride, src + sl * slot_stride,
+                               sizeof(c2_t<R>) * ((narr - 1) * arr_stride + N), cudaMemcpyDeviceToDevice, s)))
+        return e;
+    }
+  }
+  return cudaSuccess;
+}
+
 // -------------------------------------------------------------- estimate --
+
+// Knuth's merge-exchange sorting network (TAOCP vol. 3, 5.2.2, Algorithm M)
+// for N elements, generated at compile time; used through Cswap so that
+// every comparator's indices are constants (the values stay in registers).
+template <int N>
+struct SortNet {
+  static constexpr int count() {
+    if (N < 2) return 0;
+    int t = 0;
+    while ((1 << t) < N) t++;
+    int c = 0;
+    for (int p = 1 << (t - 1); p > 0; p >>= 1) {
+      int q = 1 << (t - 1), r = 0, dd = p;
+      for (;;) {
+        for (int i = 0; i + dd < N; i++)
+          if ((i & p) == r) c++;
+        if (q == p) break;
+        dd = q - p;
+        q >>= 1;
+        r = p;
+      }
+    }
+    return c;
+  }
+  static constexpr int C = count();
+  int a[C > 0 ? C : 1], b[C > 0 ? C : 1];
+  constexpr SortNet() : a(), b() {
+    if (N < 2) return;
+    int t = 0;
+    while ((1 << t) < N) t++;
+    int c = 0;
+    for (int p = 1 << (t - 1); p > 0; p >>= 1) {
+      int q = 1 << (t - 1), r = 0, dd = p;
+      for (;;) {
+        for (int i = 0; i + dd < N; i++)
+          if ((i & p) == r) {
+            a[c] = i;
+            b[c] = i + dd;
+            c++;
+          }
+        if (q == p) break;
+        dd = q - p;
+        q >>= 1;
+        r = p;
+      }
+    }
+  }
+};
+
+template <int N> struct NetOf { static constexpr SortNet<N> net{}; };
+
+template <int N, int c, int C>
+struct Cswap {
+  static __device__ __forceinline__ void run(float (&v)[N]) {
+    constexpr int i = NetOf<N>::net.a[c], j = NetOf<N>::net.b[c];
+    const float x = v[i], y = v[j];
+    v[i] = fminf(x, y);
+    v[j] = fmaxf(x, y);
+    Cswap<N, c + 1, C>::run(v);
+  }
+};
+template <int N, int C>
+struct Cswap<N, C, C> {
+  static __device__ __forceinline__ void run(float (&)[N]) {}
+};
+
+template <int N>
+__device__ __forceinline__ void sort_net(float (&v)[N]) {
+  Cswap<N, 0, SortNet<N>::C>::run(v);
+}
 
 __device__ __forceinline__ long long okey(double v) {
   long long b = __double_as_longlong(v);
   return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
 }
 
-template <typename R> struct Med;
-template <> struct Med<double> {
-  using K = long long;
-  static __device__ __forceinline__ K key(double v) { return okey(v); }
-  static __device__ __forceinline__ K pad() { return LLONG_MAX; }
-};
-template <> struct Med<float> {
-  using K = float;
-  static __device__ __forceinline__ K key(float v) { return v; }
-  static __device__ __forceinline__ K pad() { return FLT_MAX; }
+struct Slot {
+  int q, B, lq;
+  long off;
 };
 
-// value of one (candidate, loop) pair: x_samp[bucket] / filter.freq[dist],
-// with the reference's sign convention (conjugate, src/computefourier-1.0-2.0.cc:383-398)
-template <typename R>
-__device__ __forceinline__ void loop_value(const V12Dev &d, const c2_t<R> *xs, int j, unsigned f,
-                                           unsigned long long ai, R &re, R &im) {
+__device__ __forceinline__ Slot loop_slot(const V12Dev &d, int j) {
   const bool loc = j < d.L_loc;
-  const int q = loc ? d.q_loc : d.q_est;
-  const int B = loc ? d.B_loc : d.B_est;
-  const long off = loc ? (long)j * d.B_loc : (long)d.L_loc * d.B_loc + (long)(j - d.L_loc) * d.B_est;
-  const unsigned long long p = ((unsigned long long)f * ai) & ((unsigned long long)d.n - 1);
-  const int lq = dlog2(q);
-  int hashed = (int)(p >> lq);
-  int dist = (int)(p & (q - 1));
-  if (dist > (q >> 1)) {
-    hashed = (hashed + 1) & (B - 1);
-    dist -= q;
-  }
-  const int m = dist + ((q - 1) >> 1);
-  const c2_t<R> v = xs[off + hashed];
-  if constexpr (sizeof(R) == 8) {
-    const double2 *wp = (const double2 *)(loc ? d.win_loc : d.win_est) + 2 * m;
-    const double2 h = __ldg(wp);           // filter.freq entry (c, d)
-    const double den = __ldg(wp + 1).x;    // c*c + d*d
-    using A = Ar<double>;
-    re = A::div(A::add(A::mul(v.x, h.x), A::mul(v.y, h.y)), den);
-    im = A::div(A::sub(A::mul(v.x, h.y), A::mul(v.y, h.x)), den);
-  } else {
-    const float2 g = __ldg((const float2 *)(loc ? d.win_loc : d.win_est) + m);
-    re = v.x * g.x + v.y * g.y;
-    im = v.x * g.y - v.y * g.x;
-  }
+  Slot s;
+  s.q = loc ? d.q_loc : d.q_est;
+  s.B = loc ? d.B_loc : d.B_est;
+  s.lq = dlog2(s.q);
+  s.off = loc ? (long)j * d.B_loc : (long)d.L_loc * d.B_loc + (long)(j - d.L_loc) * d.B_est;
+  return s;
 }
 
-template <typename R, int LMAX>
-__global__ void __launch_bounds__(128) k_estimate(V12Dev d) {
-  using K = typename Med<R>::K;
-  const int slot = blockIdx.y;
-  const long h = (long)blockIdx.x * blockDim.x + threadIdx.x;
+// bucket and window index of frequency f in loop j
+// (computefourier-1.0-2.0.cc:370-378)
+__device__ __forceinline__ void bucket_of(const V12Dev &d, const Slot &s, unsigned f, unsigned long long ai,
+                                          int &hashed, int &m) {
+  const unsigned long long p = ((unsigned long long)f * ai) & ((unsigned long long)d.n - 1);
+  hashed = (int)(p >> s.lq);
+  int dist = (int)(p & (s.q - 1));
+  if (dist > (s.q >> 1)) {
+    hashed = (hashed + 1) & (s.B - 1);
+    dist -= s.q;
+  }
+  m = dist + ((s.q - 1) >> 1);
+}
+
+// FP32 value x_samp[bucket] / filter.freq[dist] with the reference's sign
+// (conjugate, computefourier-1.0-2.0.cc:383-398), via g = conj(h)/|h|^2.
+// scale receives (|a| + |b|)(|g.x| + |g.y|), a bound on the terms summed.
+__device__ __forceinline__ void value32(const V12Dev &d, const float2 *xs, const float2 *win_loc,
+                                        const float2 *win_est, int j, unsigned f, unsigned long long ai, float &re,
+                                        float &im, float &scale) {
+  const Slot s = loop_slot(d, j);
+  int hashed, m;
+  bucket_of(d, s, f, ai, hashed, m);
+  const float2 v = xs[s.off + hashed];
+  const float2 g = __ldg((j < d.L_loc ? win_loc : win_est) + m);
+  re = v.x * g.x + v.y * g.y;
+  im = v.x * g.y - v.y * g.x;
+  scale = (fabsf(v.x) + fabsf(v.y)) * (fabsf(g.x) + fabsf(g.y));
+}
+
+// FP64 value, the reference's exact operation sequence:
+// ((a c + b d) / (c^2 + d^2), (a d - b c) / (c^2 + d^2))
+__device__ __forceinline__ double2 value64(const V12Dev &d, const double2 *xs, int j, unsigned f,
+                                           unsigned long long ai) {
+  const Slot s = loop_slot(d, j);
+  int hashed, m;
+  bucket_of(d, s, f, ai, hashed, m);
+  const double2 v = xs[s.off + hashed];
+  const double2 *wp = (const double2 *)(j < d.L_loc ? d.win_loc : d.win_est) + 2 * m;
+  const double2 h = __ldg(wp);
+  const double den = __ldg(wp + 1).x;
+  using A = Ar<double>;
+  return make_double2(A::div(A::add(A::mul(v.x, h.x), A::mul(v.y, h.y)), den),
+                      A::div(A::sub(A::mul(v.x, h.y), A::mul(v.y, h.x)), den));
+}
+
+// Exact lower medians of all L FP64 values (used when the FP32 pre-selection
+// cannot prove which element is the median, e.g. ties).
+__device__ __noinline__ double2 median64_exact(const V12Dev &d, const double2 *xs, const int *rp, unsigned f) {
+  double vre[32], vim[32];
+  const int L = d.L;
+  for (int j = 0; j < L; j++) {
+    const double2 v = value64(d, xs, j, f, (unsigned)rp[L + j]);
+    vre[j] = v.x;
+    vim[j] = v.y;
+  }
+  const int m = (L - 1) >> 1;
+  double mre = 0, mim = 0;
+  for (int i = 0; i < L; i++) {
+    const long long ki = okey(vre[i]), kj = okey(vim[i]);
+    int rr = 0, ri = 0;
+    for (int jj = 0; jj < L; jj++) {
+      const long long a = okey(vre[jj]), b = okey(vim[jj]);
+      rr += (a < ki) || (jj < i && a == ki);
+      ri += (b < kj) || (jj < i && b == kj);
+    }
+    if (rr == m) mre = vre[i];
+    if (ri == m) mim = vim[i];
+  }
+  return make_double2(mre, mim);
+}
+
+// Candidate h of a slot: v1 hits, v2 every comb candidate.  Returns false
+// when h is past the end; publishes the count once.
+__device__ __forceinline__ bool candidate(const V12Dev &d, int slot, long h, unsigned &f) {
   int *cnt = d.counters + slot * CNT_STRIDE;
   long total;
-  unsigned f;
   if (d.version == 0) {
     total = min(cnt[CNT_HITS], d.hit_cap);
-    if (h >= total) return;
+    if (h >= total) return false;
     f = (unsigned)d.hits[(long)slot * d.hit_cap + h];
   } else {
     const int nc = cnt[CNT_COMB];
     total = (long)nc * (d.n / d.W);
-    if (h >= total) return;
+    if (h >= total) return false;
     const long rep = h / nc;
     f = (unsigned)(rep * d.W + d.comb_list[(long)slot * d.W + (h - rep * nc)]);
   }
@@ -285,46 +498,118 @@ __global__ void __launch_bounds__(128) k_estimate(V12Dev d) {
     cnt[CNT_OUT] = (int)min(total, (long)d.out_cap);
     if (total > d.out_cap) atomicOr(&cnt[CNT_ERR], ERR_OUT_OVERFLOW);
   }
-  if (h >= d.out_cap) return;
-  const int *rp = d.rparams + (long)slot * d.rp_stride;
-  const c2_t<R> *xs = (const c2_t<R> *)d.xs + (long)slot * d.xs_size;
-  R vre[LMAX], vim[LMAX];
-  K kre[LMAX], kim[LMAX];
+  return h < d.out_cap;
+}
+
+// Picks the lower-median element of v[0..Lr) (FP32 approximations whose
+// exact values lie within +-e); returns its index if it is provably the
+// exact median, else -1.
+template <int LN>
+__device__ __forceinline__ int proven_median(const float (&v)[LN], int Lr, float e) {
+  float s[LN];
 #pragma unroll
-  for (int j = 0; j < LMAX; j++) {
-    if (j < d.L) {
-      loop_value<R>(d, xs, j, f, (unsigned)rp[d.L + j], vre[j], vim[j]);
-      kre[j] = Med<R>::key(vre[j]);
-      kim[j] = Med<R>::key(vim[j]);
-    } else {
-      vre[j] = 0;
-      vim[j] = 0;
-      kre[j] = Med<R>::pad();
-      kim[j] = Med<R>::pad();
+  for (int j = 0; j < LN; j++) s[j] = v[j];
+  sort_net(s);
+  const int m = (Lr - 1) >> 1;
+  float med = 0;
+#pragma unroll
+  for (int j = 0; j < LN; j++)
+    if (j == m) med = s[j];
+  int idx = -1;
+#pragma unroll
+  for (int j = LN - 1; j >= 0; j--)
+    if (j < Lr && v[j] == med) idx = j;
+  int below = 0, above = 0;
+#pragma unroll
+  for (int j = 0; j < LN; j++) {
+    if (j < Lr && j != idx) {
+      below += (v[j] < med - 2.0f * e);
+      above += (v[j] > med + 2.0f * e);
     }
   }
-  // lower median (nth_element at (L-1)/2), real and imaginary separately
-  const int mrank = (d.L - 1) >> 1;
-  R mre = 0, mim = 0;
+  return (below == m && above == Lr - 1 - m) ? idx : -1;
+}
+
+// FP32 form: values and medians in FP32.
+template <int LN, bool EXACT>
+__global__ void __launch_bounds__(128) k_estimate32(V12Dev d) {
+  const int slot = blockIdx.y;
+  const long h = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned f;
+  if (!candidate(d, slot, h, f)) return;
+  const int Lr = EXACT ? LN : d.L;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const float2 *xs = (const float2 *)d.xs + (long)slot * d.xs_size;
+  float re[LN], im[LN];
 #pragma unroll
-  for (int i = 0; i < LMAX; i++) {
-    int rr = 0, ri = 0;
+  for (int j = 0; j < LN; j++) {
+    if (EXACT || j < Lr) {
+      float sc;
+      value32(d, xs, (const float2 *)d.win_loc, (const float2 *)d.win_est, j, f, (unsigned)rp[d.L + j], re[j],
+              im[j], sc);
+    } else {
+      re[j] = INFINITY;
+      im[j] = INFINITY;
+    }
+  }
+  sort_net(re);
+  sort_net(im);
+  const int m = (Lr - 1) >> 1;
+  float mre = 0, mim = 0;
 #pragma unroll
-    for (int jj = 0; jj < LMAX; jj++) {
-      rr += (kre[jj] < kre[i]) || (jj < i && kre[jj] == kre[i]);
-      ri += (kim[jj] < kim[i]) || (jj < i && kim[jj] == kim[i]);
+  for (int j = 0; j < LN; j++)
+    if (j == m) {
+      mre = re[j];
+      mim = im[j];
     }
-    if (i < d.L) {
-      if (rr == mrank) mre = vre[i];
-      if (ri == mrank) mim = vim[i];
+  const long o = (long)slot * d.out_cap + h;
+  d.out_idx[o] = (int)f;
+  ((float2 *)d.out_val)[o] = make_float2(mre, mim);
+}
+
+// FP64 form, bit-exact: the median element is chosen on FP32 copies with a
+// rigorous error bound, then only that element is divided in FP64 (the
+// reference's exact operation sequence); anything not provable (ties,
+// near-ties) takes the all-exact path.
+template <int LN, bool EXACT>
+__global__ void __launch_bounds__(128) k_estimate64(V12Dev d) {
+  const int slot = blockIdx.y;
+  const long h = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned f;
+  if (!candidate(d, slot, h, f)) return;
+  const int Lr = EXACT ? LN : d.L;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const float2 *xs32 = (const float2 *)d.xs32 + (long)slot * d.xs_size;
+  const double2 *xs = (const double2 *)d.xs + (long)slot * d.xs_size;
+  float re[LN], im[LN];
+  float smax = 0.f;
+#pragma unroll
+  for (int j = 0; j < LN; j++) {
+    if (EXACT || j < Lr) {
+      float sc;
+      value32(d, xs32, (const float2 *)d.win32_loc, (const float2 *)d.win32_est, j, f, (unsigned)rp[d.L + j],
+              re[j], im[j], sc);
+      smax = fmaxf(smax, sc);
+    } else {
+      re[j] = INFINITY;
+      im[j] = INFINITY;
     }
+  }
+  // |exact - approx| <= 2^-20 * scale: each FP32 operand carries one
+  // rounding (2^-24 relative), plus two products and a sum; 4x margin.
+  const float e = smax * 0x1p-20f + 1e-30f;
+  const int ir = proven_median<LN>(re, Lr, e);
+  const int ii = proven_median<LN>(im, Lr, e);
+  double2 res;
+  if (ir >= 0 && ii >= 0) {
+    res.x = value64(d, xs, ir, f, (unsigned)rp[d.L + ir]).x;
+    res.y = value64(d, xs, ii, f, (unsigned)rp[d.L + ii]).y;
+  } else {
+    res = median64_exact(d, xs, rp, f);
   }
   const long o = (long)slot * d.out_cap + h;
   d.out_idx[o] = (int)f;
-  c2_t<R> res;
-  res.x = mre;
-  res.y = mim;
-  ((c2_t<R> *)d.out_val)[o] = res;
+  ((double2 *)d.out_val)[o] = res;
 }
 
 // ---------------------------------------------------------------- scatter --
@@ -344,6 +629,7 @@ __global__ void k_scatter_dense(const int *out_idx, const c2_t<R> *out_val, cons
 // ---------------------------------------------------------------- launch --
 
 int v12_max_fft(int prec) { return prec == PREC_FP64 ? 8192 : 16384; }
+int v12_max_fft_any() { return 1 << 20; }
 
 template <typename F>
 static cudaError_t set_smem(F *kern, size_t bytes) {
@@ -405,41 +691,82 @@ static cudaError_t launch_bucket(const V12Dev &d, int nslots, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+#define SFFT_EST_KERNEL(NAME)                                                   \
+  template <int LN, bool EX>                                                    \
+  struct NAME##_k {                                                             \
+    static void go(dim3 g, cudaStream_t s, const V12Dev &d) { NAME<LN, EX><<<g, 128, 0, s>>>(d); } \
+  };
+SFFT_EST_KERNEL(k_estimate32)
+SFFT_EST_KERNEL(k_estimate64)
+#undef SFFT_EST_KERNEL
+
+template <template <int, bool> class KS>
+static cudaError_t dispatch_estimate(const V12Dev &d, dim3 grid, cudaStream_t s) {
+  switch (d.L) {
+#define SFFT_L(v) \
+  case v:         \
+    KS<v, true>::go(grid, s, d); \
+    break;
+    SFFT_L(8) SFFT_L(9) SFFT_L(10) SFFT_L(11) SFFT_L(12) SFFT_L(13) SFFT_L(14) SFFT_L(15) SFFT_L(16)
+    SFFT_L(17) SFFT_L(18) SFFT_L(19) SFFT_L(20) SFFT_L(21) SFFT_L(22) SFFT_L(23) SFFT_L(24)
+#undef SFFT_L
+    default:
+      if (d.L > 32) return cudaErrorInvalidValue;
+      KS<32, false>::go(grid, s, d);
+  }
+  return cudaGetLastError();
+}
+
 template <typename R>
 static cudaError_t launch_estimate(const V12Dev &d, int nslots, cudaStream_t s) {
   const int cap = d.version == 0 ? d.hit_cap : d.out_cap;
   dim3 grid((cap + 127) / 128, nslots);
-  if (d.L <= 12)
-    k_estimate<R, 12><<<grid, 128, 0, s>>>(d);
-  else if (d.L <= 16)
-    k_estimate<R, 16><<<grid, 128, 0, s>>>(d);
-  else if (d.L <= 24)
-    k_estimate<R, 24><<<grid, 128, 0, s>>>(d);
-  else if (d.L <= 32)
-    k_estimate<R, 32><<<grid, 128, 0, s>>>(d);
-  else
-    return cudaErrorInvalidValue;
-  return cudaGetLastError();
+  if (sizeof(R) == 8) return dispatch_estimate<k_estimate64_k>(d, grid, s);
+  return dispatch_estimate<k_estimate32_k>(d, grid, s);
 }
 
 template <typename R, typename In>
 static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageEvents *se) {
   cudaError_t e;
+  using V = c2_t<R>;
   if ((e = cudaMemsetAsync(d.counters, 0, sizeof(int) * CNT_STRIDE * nslots, s))) return e;
   mark(se, s);
   if (d.version == 1) {
     if ((e = cudaMemsetAsync(d.comb_bits, 0, sizeof(unsigned) * ((d.W + 31) >> 5) * nslots, s))) return e;
-    if ((e = launch_comb<R, In>(d, nslots, s))) return e;
+    if (!d.large_comb) {
+      if ((e = launch_comb<R, In>(d, nslots, s))) return e;
+    } else {
+      dim3 g((d.W + 255) / 256, d.comb_loops, nslots);
+      k_comb_gather<R, In><<<g, 256, 0, s>>>(d);
+      if ((e = cudaGetLastError())) return e;
+      if ((e = global_fft<R>((V *)d.comb_buf, (V *)d.comb_tmp, d.W, d.comb_loops, d.W, (long)d.comb_loops * d.W,
+                             nslots, (const V *)d.tw_comb, s)))
+        return e;
+      k_comb_select<R><<<dim3(d.comb_loops, nslots), 1024, sizeof(int) * d.num, s>>>(d);
+      if ((e = cudaGetLastError())) return e;
+      note_launches(2);
+    }
     k_comb_list<<<nslots, 1024, 0, s>>>(d);
     if ((e = cudaGetLastError())) return e;
-    note_launches(2);
+    note_launches(1);
   }
   mark(se, s);
   dim3 fg((unsigned)((d.xs_size + 255) / 256), nslots);
   k_fold<R, In><<<fg, 256, 0, s>>>(d);
   if ((e = cudaGetLastError())) return e;
   mark(se, s);
-  if ((e = launch_bucket<R>(d, nslots, s))) return e;
+  if (!d.large_buckets) {
+    if ((e = launch_bucket<R>(d, nslots, s))) return e;
+  } else {
+    V *xs = (V *)d.xs, *tmp = (V *)d.xs_tmp;
+    const long locsz = (long)d.L_loc * d.B_loc;
+    if ((e = global_fft<R>(xs, tmp, d.B_loc, d.L_loc, d.B_loc, d.xs_size, nslots, (const V *)d.tw_loc, s))) return e;
+    if ((e = global_fft<R>(xs + locsz, tmp + locsz, d.B_est, d.L_est, d.B_est, d.xs_size, nslots,
+                           (const V *)d.tw_est, s)))
+      return e;
+    k_select_vote<R><<<dim3(d.L, nslots), 1024, sizeof(int) * d.num, s>>>(d);
+    if ((e = cudaGetLastError())) return e;
+  }
   mark(se, s);
   if ((e = launch_estimate<R>(d, nslots, s))) return e;
   mark(se, s);

@@ -4,10 +4,9 @@
 //                 (computefourier-3.0.cc:96-127), the two shifts of the
 //                 contiguous Gaussian fold (:130-212) and of the permuted
 //                 Gaussian fold (:215-297), each followed by its
-//                 shared-memory FFT.  The permutation phase of the second
-//                 fold is e^{2 pi i ((b * idx) mod n) / n} from the exact
-//                 integer product, not the reference's running product
-//                 (:66-87); both describe the same phase.
+//                 shared-memory FFT.  The permuted samples of the second
+//                 fold replay the reference's running phase product
+//                 (:66-87) on one thread, so their rounding matches.
 //   k_v3_peel     one CTA per signal runs alternate_fft's estimate / peel
 //                 rounds (:784-1088): bucket estimation in parallel,
 //                 subtraction of recovered tones with FP64 atomics, and the
@@ -70,18 +69,31 @@ __global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d) {
     tw = (const double2 *)d.tw_g2;
     dst = (double2 *)d.g2 + (long)slot * 2 * d.B2;
     const int chunks = d.w2 / d.B2;
-    const unsigned long long ig = (unsigned)rp[4], ai = (unsigned)rp[1], bb = (unsigned)rp[2];
+    const int ig = rp[4], ai = rp[1], bb = rp[2];
     const double2 *taps = (const double2 *)d.taps2;
+    // permute_fourier (computefourier-3.0.cc:66-87): sample i is
+    // x[(ig + i*ai) mod n] * shift_i with shift_0 = e^{2 pi i ig b / n} and
+    // shift_{i+1} = shift_i * e^{2 pi i ai b / n}, a running product whose
+    // rounding is part of the reference's result; one thread replays it.
+    double2 *P = (double2 *)d.perm + (long)slot * (d.w2 + 2) * 2 + (long)l * (d.w2 + 2);
+    if (threadIdx.x == 0) {
+      const double a0 = 2 * kPi * ig * bb / d.n, a1 = 2 * kPi * ai * bb / d.n;
+      double2 sh = make_double2(cos(a0), sin(a0));
+      const double2 st = make_double2(cos(a1), sin(a1));
+      long index = ig % d.n;
+      const int count = chunks * N + 1;
+      for (int i = 0; i < count; i++) {
+        if (i >= l) P[i - l] = cmul<double>(ld_x(x, d.in_type, index), sh);
+        sh = cmul<double>(sh, st);
+        index = (index + ai) % d.n;
+      }
+    }
+    __syncthreads();
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
       double2 acc = make_double2(0.0, 0.0);
       for (int c = 0; c < chunks; c++) {
         const int t = c * N + b;
-        const unsigned long long idx = (ig + (unsigned long long)(t + l) * ai) & mask;
-        const unsigned long long ph = (bb * idx) & mask;
-        double s, co;
-        sincos((2.0 * kPi * (double)ph) / (double)d.n, &s, &co);
-        const double2 pv = cmul<double>(ld_x(x, d.in_type, (long)idx), make_double2(co, s));
-        acc = cadd<double>(acc, cmul<double>(pv, __ldg(taps + t)));
+        acc = cadd<double>(acc, cmul<double>(P[t], __ldg(taps + t)));
       }
       buf[b] = acc;
     }

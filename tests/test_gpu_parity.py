@@ -52,6 +52,7 @@ V12_CASES = [
     (1 << 20, 50, 2, 4, None, None),
     (1 << 22, 100, 1, 11, None, None),
     (1 << 22, 100, 2, 7, (0.1, 10.0), 20.0),    # C4 shape (metric workload)
+    (1 << 24, 50, 1, 13, None, None),           # B_loc = 16384: global-memory FFTs
     (256, 2, 1, 9, None, None),                 # smallest tuned-free domain
     (256, 2, 2, 9, None, None),
 ]
@@ -75,6 +76,26 @@ def test_v12_fp64_bit_exact(S, oracle_lib, n, k, v, seed, mag, snr):
     np.testing.assert_array_equal(xs, op.xsamp())
     if v == 2:
         np.testing.assert_array_equal(g.debug(4, n), op.comb())
+
+
+@pytest.mark.parametrize("v,prec", [(1, "fp64"), (2, "fp64"), (1, "fp32"), (2, "fp32")])
+def test_v12_global_memory_fft_path(S, oracle_lib, monkeypatch, v, prec):
+    """Bucket and comb FFTs forced through the multi-launch global-memory
+    Stockham path (as plans with more than 8192 / 16384 buckets use)."""
+    from sfft_gb300 import signals
+    monkeypatch.setenv("SFFT_GB300_MAX_SMEM_FFT", "256")
+    n, k, seed = 1 << 16, 50, 3
+    x, pos, vals = signals.make_signal(n, k, seed, snr_db=40.0)
+    op, oi, ov, g, gi, gv = _run(S, oracle_lib, n, k, v, seed, x, prec=prec)
+    if prec == "fp64":
+        np.testing.assert_array_equal(gi, oi)
+        np.testing.assert_array_equal(gv, ov)
+        L = op.loops()
+        np.testing.assert_array_equal(g.debug(2, n), op.score())
+        np.testing.assert_array_equal(g.debug(1, L * op.params["B_thresh"]).reshape(L, -1), op.J())
+    else:
+        tau = 0.5 * float(np.min(np.abs(vals)))
+        np.testing.assert_array_equal(gi[np.abs(gv) >= tau], oi[np.abs(ov) >= tau])
 
 
 @pytest.mark.parametrize("v", [1, 2])
