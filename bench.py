@@ -45,6 +45,8 @@ def args_():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--pool", type=int, default=64)
+    ap.add_argument("--only", default="all", choices=["all", "device"],
+                    help="device: only the device-resident timed legs (for profiler captures)")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -273,6 +275,12 @@ def gb300_arm(a, ws, rank, local):
     t64, per64, _, st64 = timed(p64, oval64, s64, 3, profile=True)
     t64max = max_over_ranks(ws, t64)
     value64 = ws * B * s64 / (t64max / 1e3)
+    if a.only == "device":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "solves/s", "fp64_value": value64,
+                              "only": "device", "stage_ms_per_launch_fp32": stage_table(st32),
+                              "stage_ms_per_launch_fp64": stage_table(st64)}), flush=True)
+        return
 
     # ---- single-request latency (batch of one)
     def lat(plan, oval, runs=30):

@@ -118,6 +118,9 @@ struct PlanImpl {
   sfft::V3Params p3;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
+  // host-buffer pipeline of sfft_exec_many: copies in / out on their own streams
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
   std::mutex mu;
   // constants
   DBuf taps_a, taps_b, win_a, win_b, win32_a, win32_b, tw_a, tw_b, tw_c;
@@ -371,8 +374,10 @@ sfft::V12Dev v12_view(PlanImpl &P) {
   d.counters = P.counters.as<int>();
   d.out_idx = P.out_idx.as<int>();
   d.out_val = P.out_val.p;
+  d.out_count = nullptr;
   d.hit_cap = P.hit_cap;
   d.out_cap = P.out_cap;
+  d.out_stride = P.out_cap;
   d.rparams = P.rparams.as<int>();
   d.rp_stride = P.rp_stride;
   d.inputs = (const void *const *)P.inputs.p;
@@ -417,7 +422,9 @@ sfft::V3Dev v3_view(PlanImpl &P) {
   d.counters = P.counters.as<int>();
   d.out_idx = P.out_idx.as<int>();
   d.out_val = P.out_val.p;
+  d.out_count = nullptr;
   d.out_cap = P.out_cap;
+  d.out_stride = P.out_cap;
   d.max_passes = 3000;
   d.trace = P.trace.as<double>();
   d.trace_cap = P.map_cap;
@@ -427,49 +434,127 @@ sfft::V3Dev v3_view(PlanImpl &P) {
   return d;
 }
 
+// Where a launch writes its sparse results (default: the plan's buffers).
+struct OutTarget {
+  int *idx;
+  void *val;
+  int *count;
+  long stride;
+};
+
 // Uploads draws and input pointers for `num` slots and runs the pipeline.
-bool launch(PlanImpl &P, int num, const void *const *in_dev, int in_type, cudaStream_t s) {
+template <typename T>
+void shift(T *&p, size_t per_slot, int base) {
+  if (p) p = (T *)((char *)p + per_slot * (size_t)base);
+}
+
+// Moves every per-slot pointer of a view to slot `base` (double-buffered
+// pipelines use slots [base, base + num)).
+void shift_view(PlanImpl &P, sfft::V12Dev &d, int base, bool own_out) {
+  if (!base) return;
+  const size_t cs = P.prec == sfft::PREC_FP64 ? 16 : 8;
+  shift(d.xs, cs * d.xs_size, base);
+  shift(d.xs32, 8 * d.xs_size, base);
+  shift(d.xs_tmp, cs * d.xs_size, base);
+  shift(d.comb_buf, cs * (size_t)d.comb_loops * d.W, base);
+  shift(d.comb_tmp, cs * (size_t)d.comb_loops * d.W, base);
+  shift(d.J, sizeof(int) * (size_t)d.L * d.num, base);
+  shift(d.score, sizeof(unsigned) * (size_t)d.n, base);
+  shift(d.hits, sizeof(int) * (size_t)d.hit_cap, base);
+  shift(d.comb_bits, sizeof(unsigned) * (size_t)((d.W + 31) / 32), base);
+  shift(d.comb_list, sizeof(int) * (size_t)d.W, base);
+  shift(d.counters, sizeof(int) * sfft::CNT_STRIDE, base);
+  if (own_out) {
+    shift(d.out_idx, sizeof(int) * (size_t)d.out_cap, base);
+    shift(d.out_val, cs * (size_t)d.out_cap, base);
+  }
+  shift(d.rparams, sizeof(int) * (size_t)d.rp_stride, base);
+  shift(d.inputs, sizeof(void *), base);
+}
+
+void shift_view(PlanImpl &P, sfft::V3Dev &d, int base, bool own_out) {
+  if (!base) return;
+  shift(d.man, 32 * (size_t)d.W, base);
+  shift(d.g1, 32 * (size_t)d.B1, base);
+  shift(d.g2, 32 * (size_t)d.B2, base);
+  shift(d.perm, 16 * 2 * (size_t)(d.w2 + 2), base);
+  shift(d.est_f, sizeof(int) * (size_t)d.est_cap, base);
+  shift(d.est_v, 16 * (size_t)d.est_cap, base);
+  shift(d.map_keys, sizeof(int) * (size_t)d.table_cap, base);
+  shift(d.map_vals, 16 * (size_t)d.table_cap, base);
+  shift(d.map_table, sizeof(int) * (size_t)d.map_cap, base);
+  shift(d.counters, sizeof(int) * sfft::CNT_STRIDE, base);
+  if (own_out) {
+    shift(d.out_idx, sizeof(int) * (size_t)d.out_cap, base);
+    shift(d.out_val, 16 * (size_t)d.out_cap, base);
+  }
+  shift(d.rparams, sizeof(int) * (size_t)d.rp_stride, base);
+  shift(d.inputs, sizeof(void *), base);
+  d.trace = nullptr;
+  (void)P;
+}
+
+bool launch(PlanImpl &P, int num, const void *const *in_dev, int in_type, cudaStream_t s,
+            const OutTarget *tgt = nullptr, int base = 0) {
   std::vector<int> rp((size_t)P.rp_stride * num);
   for (int i = 0; i < num; i++) {
     unsigned ep = 0;
     if (P.version < 2) {
-      if (++P.epoch[i] >= (1u << 24)) {  // wrap: clear this slot's vote counters
-        if (!cuda_ok(cudaMemsetAsync(P.score.as<unsigned>() + (size_t)i * P.n, 0, sizeof(unsigned) * P.n, s),
+      const int sl = base + i;
+      if (++P.epoch[sl] >= (1u << 24)) {  // wrap: clear this slot's vote counters
+        if (!cuda_ok(cudaMemsetAsync(P.score.as<unsigned>() + (size_t)sl * P.n, 0, sizeof(unsigned) * P.n, s),
                      "memset"))
           return false;
-        P.epoch[i] = 1;
+        P.epoch[sl] = 1;
       }
-      ep = P.epoch[i];
+      ep = P.epoch[sl];
     }
     draw_params(P, &rp[(size_t)i * P.rp_stride], ep);
   }
-  P.last_rp.assign(rp.begin(), rp.begin() + P.rp_stride);
+  if (base == 0) P.last_rp.assign(rp.begin(), rp.begin() + P.rp_stride);
   // pageable sources: the runtime stages them before returning
-  if (!cuda_ok(cudaMemcpyAsync(P.rparams.p, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice, s),
+  if (!cuda_ok(cudaMemcpyAsync(P.rparams.as<int>() + (size_t)base * P.rp_stride, rp.data(), sizeof(int) * rp.size(),
+                               cudaMemcpyHostToDevice, s),
                "params upload"))
     return false;
   std::vector<const void *> ptrs(in_dev, in_dev + num);
-  if (!cuda_ok(cudaMemcpyAsync(P.inputs.p, ptrs.data(), sizeof(void *) * num, cudaMemcpyHostToDevice, s),
+  if (!cuda_ok(cudaMemcpyAsync((const void **)P.inputs.p + base, ptrs.data(), sizeof(void *) * num,
+                               cudaMemcpyHostToDevice, s),
                "pointer upload"))
     return false;
   sfft::StageEvents *se = P.profiling ? P.take_set() : nullptr;
   bool ok;
   if (P.version < 2) {
     sfft::V12Dev d = v12_view(P);
+    shift_view(P, d, base, tgt == nullptr);
     d.in_type = in_type;
+    if (tgt) {
+      d.out_idx = tgt->idx;
+      d.out_val = tgt->val;
+      d.out_count = tgt->count;
+      d.out_stride = tgt->stride;
+    }
     ok = cuda_ok(sfft::v12_run(d, num, s, se), "v1/v2 launch");
   } else {
     sfft::V3Dev d = v3_view(P);
+    shift_view(P, d, base, tgt == nullptr);
     d.in_type = in_type;
+    if (tgt) {
+      d.out_idx = tgt->idx;
+      d.out_val = tgt->val;
+      d.out_count = tgt->count;
+      d.out_stride = tgt->stride;
+    }
     ok = cuda_ok(sfft::v3_run(d, num, s, se), "v3 launch");
   }
   if (se) P.pending.push_back(se);
   return ok;
 }
 
-bool check_device_errors(PlanImpl &P, int num) {
+bool check_device_errors(PlanImpl &P, int num, int base = 0) {
   std::vector<int> cnt((size_t)sfft::CNT_STRIDE * num);
-  if (!cuda_ok(cudaMemcpy(cnt.data(), P.counters.p, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost),
+  if (!cuda_ok(cudaMemcpy(cnt.data(), P.counters.as<int>() + (size_t)base * sfft::CNT_STRIDE, sizeof(int) * cnt.size(),
+                          cudaMemcpyDeviceToHost),
                "counters"))
     return false;
   for (int i = 0; i < num; i++) {
@@ -540,6 +625,69 @@ bool exec_dense_chunk(PlanImpl &P, int num, complex_t **in, complex_t **out) {
       return false;
   if (!cuda_ok(cudaStreamSynchronize(s), "exec")) return false;
   return check_device_errors(P, num);
+}
+
+// sfft_exec_many on host buffers: chunk c's input copies (copy_in), its
+// transform (plan stream) and its dense output copies (copy_out) overlap
+// with the neighbouring chunks; workspace, input staging and dense staging
+// are double-buffered (slot halves [0, chunk) and [chunk, 2 chunk)).
+bool exec_dense_pipelined(PlanImpl &P, int num, complex_t **in, complex_t **out, int chunk) {
+  const size_t nb = sizeof(double) * 2 * (size_t)P.n;
+  if (!ensure_slots(P, 2 * chunk)) return false;
+  if (!P.in_stage.ensure(nb * 2 * chunk) || !P.dense_stage.ensure(nb * 2 * chunk) ||
+      !P.dense_ptrs.ensure(sizeof(void *) * 2 * chunk))
+    return false;
+  cudaStream_t s = P.stream;
+  const int nchunks = (num + chunk - 1) / chunk;
+  for (int c = 0; c < nchunks; c++) {
+    const int half = c & 1, base = half * chunk, i0 = c * chunk, m = std::min(chunk, num - i0);
+    char *istage = (char *)P.in_stage.p + nb * base;
+    char *ostage = (char *)P.dense_stage.p + nb * base;
+    // inputs of chunk c may overwrite this half once chunk c-2's transform has read it
+    if (c >= 2 && !cuda_ok(cudaStreamWaitEvent(P.copy_in, P.ev_comp[half], 0), "wait")) return false;
+    for (int i = 0; i < m; i++)
+      if (!cuda_ok(cudaMemcpyAsync(istage + nb * i, in[i0 + i], nb, cudaMemcpyHostToDevice, P.copy_in), "input copy"))
+        return false;
+    if (!cuda_ok(cudaEventRecord(P.ev_in[half], P.copy_in), "event")) return false;
+    if (!cuda_ok(cudaStreamWaitEvent(s, P.ev_in[half], 0), "wait")) return false;
+    // the dense staging of this half is free once chunk c-2's output copies finished
+    if (c >= 2 && !cuda_ok(cudaStreamWaitEvent(s, P.ev_out[half], 0), "wait")) return false;
+    std::vector<const void *> dev_in(m);
+    std::vector<void *> dense(m);
+    for (int i = 0; i < m; i++) {
+      dev_in[i] = istage + nb * i;
+      dense[i] = ostage + nb * i;
+    }
+    if (!launch(P, m, dev_in.data(), sfft::IN_C128, s, nullptr, base)) return false;
+    if (!cuda_ok(cudaMemsetAsync(ostage, 0, nb * m, s), "output clear")) return false;
+    if (!cuda_ok(cudaMemcpyAsync((void **)P.dense_ptrs.p + base, dense.data(), sizeof(void *) * m,
+                                 cudaMemcpyHostToDevice, s),
+                 "pointer upload"))
+      return false;
+    const size_t cs = (P.version < 2 && P.prec == sfft::PREC_FP32) ? 8 : 16;
+    if (!cuda_ok(sfft::scatter_dense(P.out_idx.as<int>() + (size_t)base * P.out_cap,
+                                     (char *)P.out_val.p + cs * (size_t)base * P.out_cap,
+                                     P.version < 2 ? P.prec : sfft::PREC_FP64,
+                                     P.counters.as<int>() + (size_t)base * sfft::CNT_STRIDE, P.out_cap,
+                                     (void *const *)P.dense_ptrs.p + base, m, s),
+                 "scatter"))
+      return false;
+    if (!cuda_ok(cudaEventRecord(P.ev_comp[half], s), "event")) return false;
+    if (!cuda_ok(cudaStreamWaitEvent(P.copy_out, P.ev_comp[half], 0), "wait")) return false;
+    for (int i = 0; i < m; i++)
+      if (!cuda_ok(cudaMemcpyAsync(out[i0 + i], ostage + nb * i, nb, cudaMemcpyDeviceToHost, P.copy_out),
+                   "output copy"))
+        return false;
+    if (!cuda_ok(cudaEventRecord(P.ev_out[half], P.copy_out), "event")) return false;
+    if (c >= 1) {  // device errors of chunk c-1 once its transform is done
+      const int ph = (c - 1) & 1;
+      if (!cuda_ok(cudaEventSynchronize(P.ev_comp[ph]), "sync")) return false;
+      if (!check_device_errors(P, std::min(chunk, num - (c - 1) * chunk), ph * chunk)) return false;
+    }
+  }
+  if (!cuda_ok(cudaStreamSynchronize(P.copy_out), "sync") || !cuda_ok(cudaStreamSynchronize(s), "sync")) return false;
+  const int last = nchunks - 1;
+  return check_device_errors(P, num - last * chunk, (last & 1) * chunk);
 }
 
 }  // namespace
@@ -691,6 +839,14 @@ sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_o
   }
   if (!cuda_ok(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking), "stream")) return nullptr;
   if (!cuda_ok(cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming), "event")) return nullptr;
+  if (!cuda_ok(cudaStreamCreateWithFlags(&P->copy_in, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(cudaStreamCreateWithFlags(&P->copy_out, cudaStreamNonBlocking), "stream"))
+    return nullptr;
+  for (int h = 0; h < 2; h++)
+    if (!cuda_ok(cudaEventCreateWithFlags(&P->ev_in[h], cudaEventDisableTiming), "event") ||
+        !cuda_ok(cudaEventCreateWithFlags(&P->ev_comp[h], cudaEventDisableTiming), "event") ||
+        !cuda_ok(cudaEventCreateWithFlags(&P->ev_out[h], cudaEventDisableTiming), "event"))
+      return nullptr;
   if (!ensure_slots(*P, 1)) return nullptr;
   sfft_plan *plan = (sfft_plan *)std::malloc(sizeof(sfft_plan));
   if (!plan) {
@@ -717,6 +873,14 @@ void sfft_free_plan(sfft_plan *plan) {
       cudaStreamDestroy(P->stream);
     }
     if (P->done) cudaEventDestroy(P->done);
+    for (cudaStream_t st : {P->copy_in, P->copy_out})
+      if (st) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+      }
+    for (int h = 0; h < 2; h++)
+      for (cudaEvent_t e : {P->ev_in[h], P->ev_comp[h], P->ev_out[h]})
+        if (e) cudaEventDestroy(e);
     delete P;
   }
   std::free(plan);
@@ -745,6 +909,13 @@ void sfft_exec_many(sfft_plan *plan, int num, complex_t **in, complex_t **out) {
   cudaSetDevice(P->device);
   g_err.clear();
   const int chunk = std::max(1, std::min(P->max_batch, num));
+  bool all_host = num > 1;
+  for (int i = 0; i < num && all_host; i++)
+    if (is_device_ptr(in[i]) || is_device_ptr(out[i])) all_host = false;
+  if (all_host) {  // at least four chunks so that copies overlap the transforms
+    exec_dense_pipelined(*P, num, in, out, std::max(1, std::min(chunk, (num + 3) / 4)));
+    return;
+  }
   if (!ensure_slots(*P, chunk)) return;
   for (int i = 0; i < num; i += chunk) {
     const int m = std::min(chunk, num - i);
@@ -819,26 +990,15 @@ int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type
   cudaSetDevice(P->device);
   g_err.clear();
   cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
-  if (!ensure_slots(*P, std::min(num, std::max(P->max_batch, num)))) return -1;
+  if (!ensure_slots(*P, std::min(num, std::max(1, P->max_batch)))) return -1;
   if (!cuda_ok(cudaStreamWaitEvent(s, P->done, 0), "event wait")) return -1;
   const size_t cs = (P->version < 2 && P->prec == sfft::PREC_FP32) ? 8 : 16;
   for (int i0 = 0; i0 < num; i0 += P->slots) {
     const int m = std::min(P->slots, num - i0);
-    if (!launch(*P, m, in + i0, in_type, s)) return -1;
-    // gather per-slot results into the caller's strided buffers
-    for (int i = 0; i < m; i++) {
-      if (!cuda_ok(cudaMemcpyAsync(out_count + i0 + i, P->counters.as<int>() + i * sfft::CNT_STRIDE + sfft::CNT_OUT,
-                                   sizeof(int), cudaMemcpyDeviceToDevice, s),
-                   "count copy"))
-        return -1;
-    }
-    if (!cuda_ok(cudaMemcpy2DAsync(out_idx + (size_t)i0 * out_stride, sizeof(int) * out_stride, P->out_idx.p,
-                                   sizeof(int) * P->out_cap, sizeof(int) * P->out_cap, m, cudaMemcpyDeviceToDevice, s),
-                 "index copy") ||
-        !cuda_ok(cudaMemcpy2DAsync((char *)out_val + cs * (size_t)i0 * out_stride, cs * out_stride, P->out_val.p,
-                                   cs * P->out_cap, cs * P->out_cap, m, cudaMemcpyDeviceToDevice, s),
-                 "value copy"))
-      return -1;
+    // results go straight into the caller's strided buffers
+    OutTarget t{out_idx + (size_t)i0 * out_stride, (char *)out_val + cs * (size_t)i0 * out_stride, out_count + i0,
+                out_stride};
+    if (!launch(*P, m, in + i0, in_type, s, &t)) return -1;
   }
   return cuda_ok(cudaEventRecord(P->done, s), "event") ? 0 : -1;
 }

@@ -206,9 +206,17 @@ __device__ void block_top_indices_f(KeyAt keyat, int N, int num, int *__restrict
   for (int shift = BITS - 8; shift >= 0; shift -= 8) {
     for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      K k = keyat(i);
-      if ((k & mask) == prefix) atomicAdd(&hist[(int)((k >> shift) & 0xFF)], 1);
+    // warp-aggregated: lanes with the same digit add once (keys of similar
+    // magnitude share their top digits, which would serialise the atomics)
+    for (int i0 = 0; i0 < N; i0 += blockDim.x) {
+      const int i = i0 + threadIdx.x;
+      int bin = -1;
+      if (i < N) {
+        const K k = keyat(i);
+        if ((k & mask) == prefix) bin = (int)((k >> shift) & 0xFF);
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, bin);
+      if (bin >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[bin], __popc(peers));
     }
     __syncthreads();
     if (threadIdx.x < 32) {

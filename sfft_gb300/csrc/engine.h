@@ -55,9 +55,11 @@ struct V12Dev {
   unsigned *comb_bits;      // W/32 per slot
   int *comb_list;           // W per slot
   int *counters;            // CNT_STRIDE per slot
-  int *out_idx;             // out_cap per slot
-  void *out_val;            // out_cap complex per slot (R2)
+  int *out_idx;             // out_stride per slot
+  void *out_val;            // out_stride complex per slot (R2)
+  int *out_count;           // optional: per-slot coefficient count
   int hit_cap, out_cap;
+  long out_stride;
   // per-exec inputs
   const int *rparams;       // per slot: a[L], ai[L], comb_offsets[comb_loops], epoch
   int rp_stride;
@@ -99,7 +101,9 @@ struct V3Dev {
   int *counters;
   int *out_idx;
   void *out_val;
+  int *out_count;
   int out_cap;
+  long out_stride;
   int max_passes;
   double *trace;       // slot 0 only: (round, stage, key, re, im) per estimate
   int trace_cap;

@@ -160,8 +160,10 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
   d.counters = (int *)(base + o_cnt);
   d.out_idx = d_out_idx;
   d.out_val = d_out_val;
+  d.out_count = nullptr;
   d.hit_cap = hit_cap;
   d.out_cap = out_cap;
+  d.out_stride = out_cap;
   d.rparams = (const int *)(base + o_rp);
   d.rp_stride = rp_stride;
   d.inputs = (const void *const *)(base + o_in);

@@ -66,11 +66,21 @@ __global__ void __launch_bounds__(256) k_fold(V12Dev d) {
   c2_t<R> acc;
   acc.x = 0;
   acc.y = 0;
-#pragma unroll 4
-  for (int t = b; t < w; t += B) {
-    const unsigned long long idx = ((unsigned long long)t * ai) & mask;
-    const c2_t<R> xv = cvt_in<R>(__ldg(x + idx));
-    acc = cadd<R>(acc, cmul<R>(xv, __ldg(taps + t)));
+  // gathers issued 8 at a time, summed in increasing tap order
+  for (int t0 = b; t0 < w; t0 += 8 * B) {
+    c2_t<R> xv[8], hv[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int t = t0 + u * B;
+      if (t < w) {
+        const unsigned long long idx = ((unsigned long long)t * ai) & mask;
+        xv[u] = cvt_in<R>(__ldg(x + idx));
+        hv[u] = __ldg(taps + t);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (t0 + u * B < w) acc = cadd<R>(acc, cmul<R>(xv[u], hv[u]));
   }
   ((c2_t<R> *)d.xs)[(long)slot * d.xs_size + g] = acc;
 }
@@ -141,30 +151,37 @@ __global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) {
   if (threadIdx.x == 0) d.counters[slot * CNT_STRIDE + CNT_COMB] = tot.x;
 }
 
-// Voting of location loop j: positions p in [J*q - floor(q/2), +q) (mod n)
+// Voting of the location loops, one thread per (loop, selected bucket,
+// position): positions p in [J*q - floor(q/2), +q) (mod n)
 // map to frequencies f = p * a (mod n); each gets one vote (v2: only if
 // f mod W is a comb residue); reaching the threshold appends f to the
 // hits (computefourier-1.0-2.0.cc:91-116, :125-184).  Counters carry the
 // exec's epoch in their upper 24 bits, so they never need clearing.
-__device__ void vote_loop(const V12Dev &d, int slot, int j, const int *Js) {
+__global__ void __launch_bounds__(256) k_vote(V12Dev d) {
+  const int slot = blockIdx.y;
+  const int q = d.q_loc, lq = dlog2(q);
+  const long per_loop = (long)d.num << lq;
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= per_loop * d.L_loc) return;
+  const int j = (int)(g / per_loop);
+  const long e = g - (long)j * per_loop;
+  const int *Js = d.J + ((long)slot * d.L + j) * d.num;
   const int *rp = d.rparams + (long)slot * d.rp_stride;
   const unsigned long long a = (unsigned)rp[j];
   const unsigned ep = (unsigned)rp[2 * d.L + d.comb_loops];
-  const int q = d.q_loc, lq = dlog2(q);
   const long n = d.n;
   const unsigned long long mask = (unsigned long long)n - 1;
   unsigned *score = d.score + (long)slot * n;
   const unsigned *bits = d.comb_bits + (long)slot * ((d.W + 31) >> 5);
   int *cnt = d.counters + slot * CNT_STRIDE;
-  const int total = d.num << lq;
-  for (int e = threadIdx.x; e < total; e += blockDim.x) {
-    const int i = e >> lq, o = e & (q - 1);
+  {
+    const int i = (int)(e >> lq), o = (int)(e & (q - 1));
     const long low = ((long)Js[i] * q - (q >> 1) + n) & (long)mask;
     const unsigned long long p = ((unsigned long long)(low + o)) & mask;
     const unsigned f = (unsigned)((p * a) & mask);
     if (d.version == 1) {
       const unsigned r = f & (unsigned)(d.W - 1);
-      if (!((bits[r >> 5] >> (r & 31)) & 1u)) continue;
+      if (!((bits[r >> 5] >> (r & 31)) & 1u)) return;
     }
     unsigned cur = score[f], nv;
     for (;;) {
@@ -214,7 +231,6 @@ __global__ void __launch_bounds__(1024) k_bucket(V12Dev d) {
   block_top_indices<key_t<R>>(keys, B, d.num, Js, hist, scan);
   int *Jg = d.J + ((long)slot * d.L + j) * d.num;
   for (int i = threadIdx.x; i < d.num; i += blockDim.x) Jg[i] = Js[i];
-  if (loc) vote_loop(d, slot, j, Js);
 }
 
 // ------------------------------------------------- FFTs beyond one CTA --
@@ -250,7 +266,6 @@ __global__ void __launch_bounds__(1024) k_select_vote(V12Dev d) {
   block_top_indices_f<key_t<R>>([xs](int i) { return pkey(cabs2<R>(xs[i])); }, B, d.num, Js, hist, scan);
   int *Jg = d.J + ((long)slot * d.L + j) * d.num;
   for (int i = threadIdx.x; i < d.num; i += blockDim.x) Jg[i] = Js[i];
-  if (loc) vote_loop(d, slot, j, Js);
 }
 
 template <typename R, typename In>
@@ -496,6 +511,7 @@ __device__ __forceinline__ bool candidate(const V12Dev &d, int slot, long h, uns
   }
   if (h == 0) {
     cnt[CNT_OUT] = (int)min(total, (long)d.out_cap);
+    if (d.out_count) d.out_count[slot] = (int)min(total, (long)d.out_cap);
     if (total > d.out_cap) atomicOr(&cnt[CNT_ERR], ERR_OUT_OVERFLOW);
   }
   return h < d.out_cap;
@@ -535,6 +551,7 @@ template <int LN, bool EXACT>
 __global__ void __launch_bounds__(128) k_estimate32(V12Dev d) {
   const int slot = blockIdx.y;
   const long h = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const float2 *wl = (const float2 *)d.win_loc, *we = (const float2 *)d.win_est;
   unsigned f;
   if (!candidate(d, slot, h, f)) return;
   const int Lr = EXACT ? LN : d.L;
@@ -545,8 +562,7 @@ __global__ void __launch_bounds__(128) k_estimate32(V12Dev d) {
   for (int j = 0; j < LN; j++) {
     if (EXACT || j < Lr) {
       float sc;
-      value32(d, xs, (const float2 *)d.win_loc, (const float2 *)d.win_est, j, f, (unsigned)rp[d.L + j], re[j],
-              im[j], sc);
+      value32(d, xs, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
     } else {
       re[j] = INFINITY;
       im[j] = INFINITY;
@@ -562,7 +578,7 @@ __global__ void __launch_bounds__(128) k_estimate32(V12Dev d) {
       mre = re[j];
       mim = im[j];
     }
-  const long o = (long)slot * d.out_cap + h;
+  const long o = (long)slot * d.out_stride + h;
   d.out_idx[o] = (int)f;
   ((float2 *)d.out_val)[o] = make_float2(mre, mim);
 }
@@ -575,6 +591,7 @@ template <int LN, bool EXACT>
 __global__ void __launch_bounds__(128) k_estimate64(V12Dev d) {
   const int slot = blockIdx.y;
   const long h = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const float2 *wl = (const float2 *)d.win32_loc, *we = (const float2 *)d.win32_est;
   unsigned f;
   if (!candidate(d, slot, h, f)) return;
   const int Lr = EXACT ? LN : d.L;
@@ -587,8 +604,7 @@ __global__ void __launch_bounds__(128) k_estimate64(V12Dev d) {
   for (int j = 0; j < LN; j++) {
     if (EXACT || j < Lr) {
       float sc;
-      value32(d, xs32, (const float2 *)d.win32_loc, (const float2 *)d.win32_est, j, f, (unsigned)rp[d.L + j],
-              re[j], im[j], sc);
+      value32(d, xs32, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
       smax = fmaxf(smax, sc);
     } else {
       re[j] = INFINITY;
@@ -607,7 +623,7 @@ __global__ void __launch_bounds__(128) k_estimate64(V12Dev d) {
   } else {
     res = median64_exact(d, xs, rp, f);
   }
-  const long o = (long)slot * d.out_cap + h;
+  const long o = (long)slot * d.out_stride + h;
   d.out_idx[o] = (int)f;
   ((double2 *)d.out_val)[o] = res;
 }
@@ -766,6 +782,12 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
       return e;
     k_select_vote<R><<<dim3(d.L, nslots), 1024, sizeof(int) * d.num, s>>>(d);
     if ((e = cudaGetLastError())) return e;
+  }
+  {
+    const long votes = ((long)d.num * d.q_loc) * d.L_loc;
+    k_vote<<<dim3((unsigned)((votes + 255) / 256), nslots), 256, 0, s>>>(d);
+    if ((e = cudaGetLastError())) return e;
+    note_launches(1);
   }
   mark(se, s);
   if ((e = launch_estimate<R>(d, nslots, s))) return e;

@@ -355,6 +355,7 @@ __global__ void __launch_bounds__(1024) k_v3_peel(V3Dev d) {
   if (F == d.k) {  // the reference returns before writing its output (:859-860)
     if (threadIdx.x == 0) {
       cnt[CNT_OUT] = 0;
+      if (d.out_count) d.out_count[slot] = 0;
       cnt[CNT_V3] = -1;
     }
     return;
@@ -455,11 +456,12 @@ __global__ void __launch_bounds__(1024) k_v3_peel(V3Dev d) {
   const int outn = min(M, d.out_cap);
   for (int i = threadIdx.x; i < outn; i += T) {
     const int h = c.list[i];
-    d.out_idx[(long)slot * d.out_cap + i] = c.tkey[h];
-    ((double2 *)d.out_val)[(long)slot * d.out_cap + i] = c.tval[h];
+    d.out_idx[(long)slot * d.out_stride + i] = c.tkey[h];
+    ((double2 *)d.out_val)[(long)slot * d.out_stride + i] = c.tval[h];
   }
   if (threadIdx.x == 0) {
     cnt[CNT_OUT] = outn;
+    if (d.out_count) d.out_count[slot] = outn;
     cnt[CNT_V3] = rounds;
     cnt[CNT_ERR] |= s_err | (M > d.out_cap ? ERR_OUT_OVERFLOW : 0);
   }
