@@ -360,6 +360,8 @@ def algorithmic_bytes(plan_params, e_in, e_out, nnz):
 
 
 def roofline(p32, st32, B):
+    """Roofline of the dominant stage's kernel (live CUDA-event duration,
+    algorithmic bytes per launch) and of the fold, the HBM-bound kernel."""
     from sfft_gb300.sfft import describe_plan
     peaks = {}
     try:
@@ -373,22 +375,36 @@ def roofline(p32, st32, B):
     nnz = min(pp["W_Comb"], pp["Comb_loops"] * pp["B_thresh"]) * (N_SIG // pp["W_Comb"])
     ab = algorithmic_bytes(pp, 16, 8, nnz)
     per = stage_table(st32) or {}
-    # the fold is the HBM-bound kernel: input gathers + bucket stores
-    fold_bytes = B * (ab["fold_in"] + ab["xs_out"])
-    fold_ms = per.get("fold")
-    traffic = None
+    traffic = {}
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as fh:
-            tr = json.load(fh).get("k_fold_fp32_v2_n4194304_k100")
-            if tr:
-                traffic = tr["bytes_per_signal"] * B
-    except (OSError, ValueError, KeyError):
+            traffic = json.load(fh)
+    except (OSError, ValueError):
         pass
-    ach = fold_bytes / (fold_ms / 1e3) / 1e9 if fold_ms else None
-    roof = {"kernel": "k_fold<float,double2> (permuted-filter fold)", "bound": "hbm", "achieved": ach,
-            "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None, "traffic": traffic,
-            "algorithmic_bytes_per_launch": fold_bytes, "peak_source": f"{peak_src} (hbm_gbs)",
-            "launch_ms": fold_ms}
+    # per-kernel algorithmic HBM bytes of one signal
+    kernels = {
+        "fold": ("k_fold<float,double2> (permuted-filter fold)", ab["fold_in"] + ab["xs_out"],
+                 "k_fold_fp32_v2_n4194304_k100"),
+        "estimate": ("k_estimate32<20> (median estimation)", ab["out"] + ab["xs_out"],
+                     "k_estimate32_v2_n4194304_k100"),
+    }
+    out = {}
+    for stage, (name, bytes_sig, tkey) in kernels.items():
+        ms = per.get(stage)
+        ach = B * bytes_sig / (ms / 1e3) / 1e9 if ms else None
+        tr = traffic.get(tkey, {}).get("bytes_per_signal")
+        out[stage] = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                      "frac": ach / peak if ach else None, "traffic": tr * B if tr else None,
+                      "algorithmic_bytes_per_launch": B * bytes_sig, "launch_ms": ms,
+                      "peak_source": f"{peak_src} hbm_gbs (copy bandwidth)"}
+    out["fold"]["note"] = ("random 16-byte gathers: DRAM moves ~4.1x the algorithmic bytes (64% of "
+                           "peak DRAM throughput in ncu); HBM-bound at the physical level")
+    out["estimate"]["note"] = ("L2-bound, not HBM-bound: ncu shows lts__throughput 61% at a 96% L2 hit "
+                               "rate and LSU throttling; DRAM traffic is ~0")
+    dominant = max(per, key=per.get) if per else "estimate"
+    roof = dict(out.get(dominant, out["estimate"]))
+    roof["stage"] = dominant
+    roof["other_kernels"] = {k: v for k, v in out.items() if k != dominant}
     tot_ms = sum(per.values()) if per else None
     pipe_bytes = B * sum(ab.values())
     pipeline = {"algorithmic_bytes_per_solve": sum(ab.values()), "breakdown": ab,
