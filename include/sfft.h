@@ -113,6 +113,28 @@ typedef struct sfft_options sfft_options;
 sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_optimization,
                              const sfft_options *opt);
 
+/* Constants of a v1/v2 plan: what the reference reads from its parameter
+ * tables (src/parameters.cc).  Plans made from them are not the
+ * reference's plans unless the values equal the table's. */
+struct sfft_params
+{
+  double Bcst_loc, Bcst_est, Comb_cst;
+  int loc_loops, est_loops, threshold_loops, comb_loops;
+  double tolerance_loc, tolerance_est;
+};
+typedef struct sfft_params sfft_params;
+
+/* A v1/v2 plan with explicit constants (params == NULL: the reference's). */
+sfft_plan *sfft_make_plan_params(int n, int k, enum sfft_version version, const sfft_params *params,
+                                 const sfft_options *opt);
+
+/* The plan's own CUDA stream (a cudaStream_t): work submitted with a NULL
+ * stream runs there. */
+void *sfft_plan_stream(const sfft_plan *plan);
+
+/* Device memory a plan holds (constants and workspace), in bytes. */
+long sfft_plan_footprint(const sfft_plan *plan);
+
 /* Message of the last failure on this thread ("" if none). */
 const char *sfft_last_error(void);
 
@@ -131,6 +153,14 @@ long sfft_exec_sparse(sfft_plan *plan, const complex_t *in, int *out_idx, comple
  * (NULL = the plan's stream).  Returns 0 or -1. */
 int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type, int *out_idx,
                     void *out_val, int *out_count, long out_stride, void *stream);
+
+/* As sfft_exec_batch, with the random draws of signal s taken from
+ * private generators seeded with seeds[s] exactly as srandom(seeds[s]);
+ * srand48(seeds[s]) would seed the reference's (seeds == NULL: the global
+ * glibc streams).  A signal's result then does not depend on the batch it
+ * runs in. */
+int sfft_exec_batch_ex(sfft_plan *plan, int num, const void *const *in, int in_type, const unsigned *seeds,
+                       int *out_idx, void *out_val, int *out_count, long out_stride, void *stream);
 
 /* Waits for the plan's work and reports device-side errors: 0 or -1. */
 int sfft_sync(sfft_plan *plan);
@@ -171,6 +201,36 @@ long sfft_kernel_launches(void);
  * race.  Returns 0, or -1 with sfft_last_error() set. */
 long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type, int *d_out_idx, void *d_out_val,
                        long cap, int *d_status, void *stream);
+
+/* ---- serving: continuous batching on one GPU ---------------------------- */
+
+typedef struct sfft_server sfft_server;
+struct sfft_server_options
+{
+  int device;                   /* CUDA device, -1 = current */
+  int max_batch;                /* transforms per batch of one plan (0: 32) */
+  long hbm_budget_bytes;        /* device memory for plans + batches (0: 80% of free) */
+  int k_round;                  /* 1: round k up to the grid ceil(8 * 2^(j/4)) */
+  int tune_invalid;             /* 1: v1/v2 (n, k) outside the reference's domain get tuned constants */
+};
+typedef struct sfft_server_options sfft_server_options;
+
+sfft_server *sfft_server_create(const sfft_server_options *opt);
+void sfft_server_destroy(sfft_server *s);
+/* Queues one transform of `in` (device or host, kept alive by the caller
+ * until the request completes); returns its id, or -1. */
+long sfft_server_submit(sfft_server *s, int n, int k, enum sfft_version version, int precision, const void *in,
+                        int in_type, unsigned seed);
+/* Waits for request `id`; writes its coefficients (host or device buffers,
+ * values as complex128) and the submit-to-completion latency.  Returns the
+ * number of coefficients, or -1. */
+long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val, long cap, double *latency_ms);
+/* Device bytes the server reserves for a plan of this shape with
+ * `max_batch` slots (its admission estimate), or -1. */
+long sfft_server_plan_bytes(int n, int k, enum sfft_version version, int precision, int max_batch);
+/* batches, plans made, plans evicted, deferrals, cached plans, bytes held,
+ * budget, queued requests. */
+int sfft_server_stats(sfft_server *s, long *stats, int nstats);
 
 /* Host-only plan queries (no GPU needed): the parameters a plan for
  * (n, k, version) would use, as the reference computes them.  fields:

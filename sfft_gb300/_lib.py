@@ -22,6 +22,18 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device", ctypes.c_int), ("max_batch", ctypes.c_int)]
 
 
+class Params(ctypes.Structure):
+    _fields_ = [("Bcst_loc", ctypes.c_double), ("Bcst_est", ctypes.c_double), ("Comb_cst", ctypes.c_double),
+                ("loc_loops", ctypes.c_int), ("est_loops", ctypes.c_int), ("threshold_loops", ctypes.c_int),
+                ("comb_loops", ctypes.c_int), ("tolerance_loc", ctypes.c_double),
+                ("tolerance_est", ctypes.c_double)]
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("max_batch", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_long),
+                ("k_round", ctypes.c_int), ("tune_invalid", ctypes.c_int)]
+
+
 class Plan(ctypes.Structure):
     _fields_ = [("version", ctypes.c_int), ("n", ctypes.c_uint), ("k", ctypes.c_uint),
                 ("data", ctypes.c_void_p)]
@@ -81,6 +93,25 @@ def load(build_if_missing=False):
     L.sfft_profile.argtypes = [PP, ci]
     L.sfft_profile_read.restype = cl
     L.sfft_profile_read.argtypes = [PP, ctypes.POINTER(ctypes.c_double), ci]
+    L.sfft_make_plan_params.restype = PP
+    L.sfft_make_plan_params.argtypes = [ci, ci, ci, ctypes.POINTER(Params), ctypes.POINTER(Options)]
+    L.sfft_plan_footprint.restype = cl
+    L.sfft_plan_footprint.argtypes = [PP]
+    L.sfft_exec_batch_ex.restype = ci
+    L.sfft_exec_batch_ex.argtypes = [PP, ci, vp, ci, vp, vp, vp, vp, cl, vp]
+    L.sfft_plan_stream.restype = vp
+    L.sfft_plan_stream.argtypes = [PP]
+    L.sfft_server_create.restype = vp
+    L.sfft_server_create.argtypes = [ctypes.POINTER(ServerOptions)]
+    L.sfft_server_destroy.argtypes = [vp]
+    L.sfft_server_submit.restype = cl
+    L.sfft_server_submit.argtypes = [vp, ci, ci, ci, ci, vp, ci, ctypes.c_uint]
+    L.sfft_server_wait.restype = cl
+    L.sfft_server_wait.argtypes = [vp, cl, vp, vp, cl, ctypes.POINTER(ctypes.c_double)]
+    L.sfft_server_plan_bytes.restype = cl
+    L.sfft_server_plan_bytes.argtypes = [ci, ci, ci, ci, ci]
+    L.sfft_server_stats.restype = ci
+    L.sfft_server_stats.argtypes = [vp, ctypes.POINTER(cl), ci]
     L.sfft_exec_noalloc.restype = cl
     L.sfft_exec_noalloc.argtypes = [PP, vp, ci, vp, vp, cl, vp, vp]
     L.sfft_kernel_launches.restype = cl

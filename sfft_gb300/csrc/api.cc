@@ -295,21 +295,52 @@ bool ensure_slots(PlanImpl &P, int want) {
 
 // ------------------------------------------------------------------ RNG --
 
+// Source of the reference's random numbers: glibc's global random() /
+// drand48() streams (what sfft_exec uses, like the reference), or private
+// reentrant copies seeded per transform (random_r / drand48_r with the
+// state srandom(seed) / srand48(seed) would give), so that a transform's
+// draws do not depend on what else runs.
+struct Rng {
+  bool seeded = false;
+  struct random_data rd;
+  char state[128];
+  struct drand48_data dd;
+  void seed(unsigned s) {
+    seeded = true;
+    std::memset(&rd, 0, sizeof rd);
+    std::memset(state, 0, sizeof state);
+    initstate_r(s, state, sizeof state, &rd);
+    srand48_r((long)s, &dd);
+  }
+  long rnd() {
+    if (!seeded) return random();
+    int32_t r;
+    random_r(&rd, &r);
+    return r;
+  }
+  double d48() {
+    if (!seeded) return drand48();
+    double x;
+    drand48_r(&dd, &x);
+    return x;
+  }
+};
+
 // Draws of one transform, in the reference's order.
-void draw_params(const PlanImpl &P, int *rp, unsigned epoch) {
+void draw_params(const PlanImpl &P, int *rp, unsigned epoch, Rng &g) {
   const int n = P.n;
   if (P.version < 2) {
     const int L = L12(P);
     for (int i = 0; i < L; i++) {  // src/computefourier-1.0-2.0.cc:465-474
       int a = 0;
-      while (gcd_ref(a, n) != 1) a = (int)(random() % n);
+      while (gcd_ref(a, n) != 1) a = (int)(g.rnd() % n);
       rp[i] = a;
       rp[L + i] = mod_inverse_ref(a, n);
     }
     for (int c = 0; c < P.p12.Comb_loops; c++) {  // :62, once per Comb_Filt call
       if (P.version == 1) {
         const int sigma = n / P.p12.W_Comb;
-        rp[2 * L + c] = (int)(unsigned)std::floor(drand48() * sigma);
+        rp[2 * L + c] = (int)(unsigned)std::floor(g.d48() * sigma);
       } else {
         rp[2 * L + c] = 0;
       }
@@ -317,13 +348,18 @@ void draw_params(const PlanImpl &P, int *rp, unsigned epoch) {
     rp[2 * L + P.p12.Comb_loops] = (int)epoch;
   } else {  // src/computefourier-3.0.cc:800-810
     int a = 0;
-    while (gcd_ref(a, n) != 1) a = (int)(random() % n);
+    while (gcd_ref(a, n) != 1) a = (int)(g.rnd() % n);
     rp[0] = a;
     rp[1] = mod_inverse_ref(a, n);
-    rp[2] = (int)(random() % n);
-    rp[3] = (int)(unsigned)std::floor(drand48() * n);
-    rp[4] = (int)(unsigned)std::floor(drand48() * n);
+    rp[2] = (int)(g.rnd() % n);
+    rp[3] = (int)(unsigned)std::floor(g.d48() * n);
+    rp[4] = (int)(unsigned)std::floor(g.d48() * n);
   }
+}
+
+void draw_params(const PlanImpl &P, int *rp, unsigned epoch) {
+  Rng g;
+  draw_params(P, rp, epoch, g);
 }
 
 // ---------------------------------------------------------------- launch --
@@ -495,7 +531,7 @@ void shift_view(PlanImpl &P, sfft::V3Dev &d, int base, bool own_out) {
 }
 
 bool launch(PlanImpl &P, int num, const void *const *in_dev, int in_type, cudaStream_t s,
-            const OutTarget *tgt = nullptr, int base = 0) {
+            const OutTarget *tgt = nullptr, int base = 0, const unsigned *seeds = nullptr) {
   std::vector<int> rp((size_t)P.rp_stride * num);
   for (int i = 0; i < num; i++) {
     unsigned ep = 0;
@@ -509,7 +545,9 @@ bool launch(PlanImpl &P, int num, const void *const *in_dev, int in_type, cudaSt
       }
       ep = P.epoch[sl];
     }
-    draw_params(P, &rp[(size_t)i * P.rp_stride], ep);
+    Rng g;
+    if (seeds) g.seed(seeds[i]);
+    draw_params(P, &rp[(size_t)i * P.rp_stride], ep, g);
   }
   if (base == 0) P.last_rp.assign(rp.begin(), rp.begin() + P.rp_stride);
   // pageable sources: the runtime stages them before returning
@@ -747,9 +785,46 @@ void sfft_free(void *p) {
 
 const char *sfft_last_error(void) { return g_err.c_str(); }
 
+static sfft_plan *make_plan_impl(int n, int k, enum sfft_version version, const sfft_options *opt,
+                                 const sfft::V12Knobs *knobs);
+
 sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_optimization,
                              const sfft_options *opt) {
   (void)fftw_optimization;
+  return make_plan_impl(n, k, version, opt, nullptr);
+}
+
+sfft_plan *sfft_make_plan_params(int n, int k, enum sfft_version version, const sfft_params *params,
+                                 const sfft_options *opt) {
+  if (!params) return make_plan_impl(n, k, version, opt, nullptr);
+  if (version == SFFT_VERSION_3) {
+    set_err("explicit parameters apply to v1/v2 plans");
+    return nullptr;
+  }
+  if (params->loc_loops < 1 || params->est_loops < 0 || params->threshold_loops < 1 ||
+      params->threshold_loops > params->loc_loops || params->comb_loops < 1 || params->comb_loops > 8 ||
+      params->Bcst_loc <= 0 || params->Bcst_est <= 0 || params->Comb_cst <= 0 ||
+      !(params->tolerance_loc > 0 && params->tolerance_loc < 1) ||
+      !(params->tolerance_est > 0 && params->tolerance_est < 1)) {
+    set_err("invalid plan parameters");
+    return nullptr;
+  }
+  sfft::V12Knobs kn;
+  kn.set = true;
+  kn.Bcst_loc = params->Bcst_loc;
+  kn.Bcst_est = params->Bcst_est;
+  kn.Comb_cst = params->Comb_cst;
+  kn.loc_loops = params->loc_loops;
+  kn.est_loops = params->est_loops;
+  kn.threshold_loops = params->threshold_loops;
+  kn.comb_loops = params->comb_loops;
+  kn.tolerance_loc = params->tolerance_loc;
+  kn.tolerance_est = params->tolerance_est;
+  return make_plan_impl(n, k, version, opt, &kn);
+}
+
+static sfft_plan *make_plan_impl(int n, int k, enum sfft_version version, const sfft_options *opt,
+                                 const sfft::V12Knobs *knobs) {
   g_err.clear();
   if (version != SFFT_VERSION_1 && version != SFFT_VERSION_2 && version != SFFT_VERSION_3) {
     set_err("unknown sFFT version");
@@ -785,7 +860,7 @@ sfft_plan *sfft_make_plan_ex(int n, int k, enum sfft_version version, int fftw_o
   std::string err;
   sfft::HostFilter fa, fb;
   if (P->version < 2) {
-    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, P->version == 1, P->p12, fa, fb, err)) {
+    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, P->version == 1, P->p12, fa, fb, err, knobs)) {
       set_err(err);
       return nullptr;
     }
@@ -886,6 +961,28 @@ void sfft_free_plan(sfft_plan *plan) {
   std::free(plan);
 }
 
+void *sfft_plan_stream(const sfft_plan *plan) {
+  const PlanImpl *P = plan ? (const PlanImpl *)plan->data : nullptr;
+  return P ? (void *)P->stream : nullptr;
+}
+
+long sfft_plan_footprint(const sfft_plan *plan) {
+  const PlanImpl *P = plan ? (const PlanImpl *)plan->data : nullptr;
+  if (!P) {
+    set_err("null plan");
+    return -1;
+  }
+  const DBuf *bufs[] = {&P->taps_a, &P->taps_b, &P->win_a, &P->win_b, &P->win32_a, &P->win32_b, &P->tw_a,
+                        &P->tw_b, &P->tw_c, &P->xs, &P->xs32, &P->xs_tmp, &P->comb_buf, &P->comb_tmp, &P->J,
+                        &P->score, &P->hits, &P->comb_bits, &P->comb_list, &P->counters, &P->out_idx,
+                        &P->out_val, &P->man, &P->g1, &P->g2, &P->perm, &P->est_f, &P->est_v, &P->map_keys,
+                        &P->map_vals, &P->map_list, &P->rparams, &P->inputs, &P->dense_ptrs, &P->in_stage,
+                        &P->dense_stage, &P->trace};
+  long total = 0;
+  for (const DBuf *b : bufs) total += (long)b->bytes;
+  return total;
+}
+
 long sfft_output_capacity(const sfft_plan *plan) {
   const PlanImpl *P = plan ? (const PlanImpl *)plan->data : nullptr;
   if (!P) {
@@ -977,6 +1074,11 @@ long sfft_exec_sparse(sfft_plan *plan, const complex_t *in, int *out_idx, comple
 
 int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type, int *out_idx, void *out_val,
                     int *out_count, long out_stride, void *stream) {
+  return sfft_exec_batch_ex(plan, num, in, in_type, nullptr, out_idx, out_val, out_count, out_stride, stream);
+}
+
+int sfft_exec_batch_ex(sfft_plan *plan, int num, const void *const *in, int in_type, const unsigned *seeds,
+                       int *out_idx, void *out_val, int *out_count, long out_stride, void *stream) {
   PlanImpl *P = impl(plan);
   if (!P || num < 1 || !in || !out_idx || !out_val || !out_count || out_stride < 0) {
     set_err("invalid arguments");
@@ -998,7 +1100,7 @@ int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type
     // results go straight into the caller's strided buffers
     OutTarget t{out_idx + (size_t)i0 * out_stride, (char *)out_val + cs * (size_t)i0 * out_stride, out_count + i0,
                 out_stride};
-    if (!launch(*P, m, in + i0, in_type, s, &t)) return -1;
+    if (!launch(*P, m, in + i0, in_type, s, &t, 0, seeds ? seeds + i0 : nullptr)) return -1;
   }
   return cuda_ok(cudaEventRecord(P->done, s), "event") ? 0 : -1;
 }

@@ -320,14 +320,24 @@ const Row *find_row(const Row (&t)[L], int key) {
 }  // namespace
 
 int build_v12_plan(unsigned n, unsigned k, bool comb, V12Params &p, HostFilter &loc,
-                   HostFilter &est, std::string &err) {
+                   HostFilter &est, std::string &err, const V12Knobs *knobs) {
   double Bcst_loc = 1, Bcst_est = 1, Comb_cst = 2;
   int loc_loops = 4, est_loops = 16, threshold_loops = 3, comb_loops = 1;
   double tolerance_loc = 1.e-8, tolerance_est = 1.e-8;
   // src/sfft.cc:316-327: k > 50 consults the per-k table with n as the key
   const Row *r = (k > 50) ? (comb ? find_row(kKComb, (int)n) : find_row(kKPlain, (int)n))
                           : (comb ? find_row(kNComb, (int)n) : find_row(kNPlain, (int)n));
-  if (r) {
+  if (knobs && knobs->set) {
+    Bcst_loc = knobs->Bcst_loc;
+    Bcst_est = knobs->Bcst_est;
+    Comb_cst = knobs->Comb_cst;
+    comb_loops = knobs->comb_loops;
+    est_loops = knobs->est_loops;
+    loc_loops = knobs->loc_loops;
+    threshold_loops = knobs->threshold_loops;
+    tolerance_loc = knobs->tolerance_loc;
+    tolerance_est = knobs->tolerance_est;
+  } else if (r) {
     Bcst_loc = r->bl;
     Bcst_est = r->be;
     Comb_cst = r->cc;

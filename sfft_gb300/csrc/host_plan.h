@@ -31,10 +31,19 @@ struct V3Params {
   int W_Man = 0, B_g1 = 0, w_g1 = 0, B_g2 = 0, w_g2 = 0;
 };
 
+// Tunable constants of a v1/v2 plan (the quantities the reference takes
+// from src/parameters.cc).  When `set`, they replace the table lookup.
+struct V12Knobs {
+  bool set = false;
+  double Bcst_loc = 1, Bcst_est = 1, Comb_cst = 2;
+  int loc_loops = 4, est_loops = 16, threshold_loops = 3, comb_loops = 1;
+  double tolerance_loc = 1e-8, tolerance_est = 1e-8;
+};
+
 // Returns 0, or -1 with `err` set when (n, k) is outside the domain on
 // which the reference's algorithm is defined.
 int build_v12_plan(unsigned n, unsigned k, bool comb, V12Params &p, HostFilter &loc,
-                   HostFilter &est, std::string &err);
+                   HostFilter &est, std::string &err, const V12Knobs *knobs = nullptr);
 int build_v3_plan(unsigned n, unsigned k, V3Params &p, HostFilter &g1, HostFilter &g2,
                   std::string &err);
 
