@@ -232,6 +232,26 @@ long sfft_server_plan_bytes(int n, int k, enum sfft_version version, int precisi
  * budget, queued requests. */
 int sfft_server_stats(sfft_server *s, long *stats, int nstats);
 
+/* ---- signals of different shapes in one CUDA graph ---------------------- */
+
+/* sfft_exec_many for `num` signals whose (n[i], k[i], version[i],
+ * precision[i]) may all differ (precision may be NULL: FP64).  Signals of
+ * one shape share a plan and run batched; all groups run concurrently as
+ * branches of one CUDA graph that later calls replay.  tune_invalid: v1/v2
+ * shapes outside the reference's domain get tuned constants. */
+typedef struct sfft_mixed sfft_mixed;
+sfft_mixed *sfft_mixed_create(int num, const int *n, const int *k, const int *version, const int *precision,
+                              int in_type, int tune_invalid, int device);
+/* One execution: in[i] device pointers; seeds (or NULL) as in
+ * sfft_exec_batch_ex.  Asynchronous; sfft_mixed_sync waits. */
+int sfft_mixed_exec(sfft_mixed *m, const void *const *in, const unsigned *seeds);
+int sfft_mixed_sync(sfft_mixed *m);
+/* Device pointers to signal s's result (indices, values of value_bytes =
+ * 16 (complex128) or 8 (complex64) each, capacity); returns its count. */
+int sfft_mixed_result(sfft_mixed *m, int s, const int **idx, const void **val, int *value_bytes, long *cap);
+int sfft_mixed_groups(const sfft_mixed *m);
+void sfft_mixed_destroy(sfft_mixed *m);
+
 /* Host-only plan queries (no GPU needed): the parameters a plan for
  * (n, k, version) would use, as the reference computes them.  fields:
  * v1/v2: B_loc, B_thresh, B_est, W_Comb, Comb_loops, loops_loc,

@@ -24,7 +24,7 @@ CU_SOURCES = ["v12.cu", "v3.cu", "noalloc.cu"]
 # v3 reproduces the reference's phase arguments (up to ~1e12 rad), whose
 # last-ulp rounding matters: no multiply-add contraction in that file.
 CU_EXTRA = {"v3.cu": ["--fmad=false"]}
-CC_SOURCES = ["api.cc", "host_plan.cc", "serve.cc"]
+CC_SOURCES = ["api.cc", "host_plan.cc", "serve.cc", "mixed.cc"]
 HEADERS = ["common.cuh", "engine.h", "host_plan.h"]
 
 

@@ -135,6 +135,11 @@ struct PlanImpl {
   int large_b = 0, large_c = 0;  // FFTs longer than one CTA's shared memory
   int rp_stride = 0;
   std::vector<int> last_rp;  // draws of the last exec (slot 0)
+  // page-locked staging for graph replays (draws and input pointers are
+  // written here by the host and copied by captured memcpy nodes)
+  int *h_rp = nullptr;
+  const void **h_in = nullptr;
+  int staged_slots = 0;
   // stage timing (sfft_profile): event sets of launches not yet harvested
   bool profiling = false;
   std::vector<sfft::StageEvents *> free_sets;
@@ -144,6 +149,8 @@ struct PlanImpl {
   ~PlanImpl() {
     for (auto *e : free_sets) destroy(e);
     for (auto *e : pending) destroy(e);
+    if (h_rp) cudaFreeHost(h_rp);
+    if (h_in) cudaFreeHost((void *)h_in);
   }
   static void destroy(sfft::StageEvents *e) {
     for (int i = 0; i < 8; i++) cudaEventDestroy(e->ev[i]);
@@ -750,6 +757,86 @@ void plan_draw(sfft_plan *plan, int *rp, unsigned epoch) { draw_params(*impl(pla
 int plan_device(sfft_plan *plan) { return impl(plan)->device; }
 
 void set_last_error(const char *m) { set_err(m); }
+
+// ----------------------------------------------- graph-capturable launches
+
+bool plan_enable_staging(sfft_plan *plan, int slots) {
+  PlanImpl *P = impl(plan);
+  if (!P) return false;
+  std::lock_guard<std::mutex> g(P->mu);
+  cudaSetDevice(P->device);
+  if (!ensure_slots(*P, slots)) return false;
+  if (P->staged_slots >= slots) return true;
+  if (P->h_rp) cudaFreeHost(P->h_rp);
+  if (P->h_in) cudaFreeHost((void *)P->h_in);
+  P->h_rp = nullptr;
+  P->h_in = nullptr;
+  if (!cuda_ok(cudaMallocHost((void **)&P->h_rp, sizeof(int) * (size_t)P->rp_stride * slots), "staging") ||
+      !cuda_ok(cudaMallocHost((void **)&P->h_in, sizeof(void *) * (size_t)slots), "staging"))
+    return false;
+  P->staged_slots = slots;
+  return true;
+}
+
+// Host side of a staged launch: the draws (from per-signal seeds) and the
+// input pointers of `num` signals go into the page-locked staging.
+bool plan_stage(sfft_plan *plan, int num, const void *const *in, const unsigned *seeds) {
+  PlanImpl *P = impl(plan);
+  if (!P || num > P->staged_slots) return false;
+  std::lock_guard<std::mutex> g(P->mu);
+  for (int i = 0; i < num; i++) {
+    unsigned ep = 0;
+    if (P->version < 2) {
+      if (++P->epoch[i] >= (1u << 24)) {
+        // counters of this slot must be cleared: done synchronously here,
+        // outside any capture (a replay is never in flight at this point)
+        if (!cuda_ok(cudaMemset(P->score.as<unsigned>() + (size_t)i * P->n, 0, sizeof(unsigned) * P->n), "memset"))
+          return false;
+        P->epoch[i] = 1;
+      }
+      ep = P->epoch[i];
+    }
+    Rng r;
+    if (seeds) r.seed(seeds[i]);
+    draw_params(*P, P->h_rp + (size_t)i * P->rp_stride, ep, r);
+    P->h_in[i] = in[i];
+  }
+  return true;
+}
+
+// Device side of a staged launch, capturable into a CUDA graph: copies the
+// staging, then the batched pipeline writing into the given outputs.
+bool plan_launch_staged(sfft_plan *plan, int num, int in_type, int *out_idx, void *out_val, int *out_count,
+                        long stride, cudaStream_t s) {
+  PlanImpl *P = impl(plan);
+  if (!P || num > P->staged_slots) return false;
+  std::lock_guard<std::mutex> g(P->mu);
+  if (!cuda_ok(cudaMemcpyAsync(P->rparams.p, P->h_rp, sizeof(int) * (size_t)P->rp_stride * num,
+                               cudaMemcpyHostToDevice, s),
+               "params upload") ||
+      !cuda_ok(cudaMemcpyAsync(P->inputs.p, P->h_in, sizeof(void *) * num, cudaMemcpyHostToDevice, s),
+               "pointer upload"))
+    return false;
+  if (P->version < 2) {
+    sfft::V12Dev d = v12_view(*P);
+    d.in_type = in_type;
+    d.out_idx = out_idx;
+    d.out_val = out_val;
+    d.out_count = out_count;
+    d.out_stride = stride;
+    return cuda_ok(sfft::v12_run(d, num, s, nullptr), "v1/v2 launch");
+  }
+  sfft::V3Dev d = v3_view(*P);
+  d.in_type = in_type;
+  d.out_idx = out_idx;
+  d.out_val = out_val;
+  d.out_count = out_count;
+  d.out_stride = stride;
+  d.trace = nullptr;
+  return cuda_ok(sfft::v3_run(d, num, s, nullptr), "v3 launch");
+}
+
+
 
 }  // namespace sfft
 

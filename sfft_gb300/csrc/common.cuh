@@ -17,6 +17,10 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace sfft {
 
 // ---------------------------------------------------------------- types --
@@ -322,6 +326,26 @@ __device__ __forceinline__ void stockham_stage(const c2_t<R> *__restrict__ src, 
   dst[base + Ns] = cadd<R>(t1, u3);
   dst[base + 2 * Ns] = csub<R>(t0, t2);
   dst[base + 3 * Ns] = csub<R>(t1, u3);
+}
+
+// Raises a kernel's dynamic shared-memory limit on the current device once
+// (per size it needs), so that later launches, including ones captured
+// into CUDA graphs, make no attribute call.
+template <typename F>
+inline cudaError_t set_smem(F *kern, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e) return e;
+  std::lock_guard<std::mutex> g(mu);
+  const auto key = std::make_pair(dev, (const void *)kern);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) done[key] = bytes;
+  return e;
 }
 
 }  // namespace sfft

@@ -481,3 +481,7 @@ int sfft_server_stats(sfft_server *s, long *stats, int nstats) {
 }
 
 }  // extern "C"
+
+namespace sfft {
+bool tuned_params_for(int n, int k, sfft_params &p) { return tuned_params(n, k, p); }
+}  // namespace sfft

@@ -647,12 +647,6 @@ __global__ void k_scatter_dense(const int *out_idx, const c2_t<R> *out_val, cons
 int v12_max_fft(int prec) { return prec == PREC_FP64 ? 8192 : 16384; }
 int v12_max_fft_any() { return 1 << 20; }
 
-template <typename F>
-static cudaError_t set_smem(F *kern, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
-  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
 static void fft_shape(int N, int &T, int &per) {
   T = N / 4;
   if (T > 1024) T = 1024;

@@ -485,15 +485,11 @@ cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t s, StageEvents *se) 
   mark(se, s);
   switch (per) {
     case 1:
-      if (sm > 48 * 1024 &&
-          (e = cudaFuncSetAttribute(k_v3_filters<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)))
-        return e;
+      if ((e = set_smem(k_v3_filters<1>, sm))) return e;
       k_v3_filters<1><<<grid, T, sm, s>>>(d);
       break;
     case 2:
-      if (sm > 48 * 1024 &&
-          (e = cudaFuncSetAttribute(k_v3_filters<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)))
-        return e;
+      if ((e = set_smem(k_v3_filters<2>, sm))) return e;
       k_v3_filters<2><<<grid, T, sm, s>>>(d);
       break;
     default:
