@@ -333,7 +333,9 @@ __device__ __forceinline__ void stockham_stage(const c2_t<R> *__restrict__ src, 
 // into CUDA graphs, make no attribute call.
 template <typename F>
 inline cudaError_t set_smem(F *kern, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
+  // below 48 KB no opt-in is needed, as long as the kernel's static shared
+  // memory leaves room: opt in from 32 KB on
+  if (bytes <= 32 * 1024) return cudaSuccess;
   static std::mutex mu;
   static std::map<std::pair<int, const void *>, size_t> done;
   int dev = 0;
@@ -345,6 +347,24 @@ inline cudaError_t set_smem(F *kern, size_t bytes) {
   if (it != done.end() && it->second >= bytes) return cudaSuccess;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e == cudaSuccess) done[key] = bytes;
+  return e;
+}
+
+// Sets a kernel attribute on the current device once, so that later
+// launches (including captured ones) make no attribute call.
+template <typename F>
+inline cudaError_t set_attr_once(F *kern, cudaFuncAttribute attr, int value) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, int> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e) return e;
+  std::lock_guard<std::mutex> g(mu);
+  const auto key = std::make_pair(dev * 64 + (int)attr, (const void *)kern);
+  auto it = done.find(key);
+  if (it != done.end() && it->second == value) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, attr, value);
+  if (e == cudaSuccess) done[key] = value;
   return e;
 }
 

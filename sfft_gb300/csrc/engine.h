@@ -23,7 +23,7 @@ enum InType { IN_C128 = 0, IN_C64 = 1 };
 
 // Per-slot counters (one block of ints per slot, zeroed before each exec).
 enum Counter { CNT_HITS = 0, CNT_COMB = 1, CNT_OUT = 2, CNT_ERR = 3, CNT_VOTED = 4, CNT_V3 = 5,
-               CNT_TRACE = 6, CNT_STRIDE = 16 };
+               CNT_TRACE = 6, CNT_EST = 7, CNT_STRIDE = 16 };
 
 // Error bits reported in counters[CNT_ERR].
 enum ErrBits { ERR_HIT_OVERFLOW = 1, ERR_OUT_OVERFLOW = 2, ERR_V3_NOCONVERGE = 4, ERR_V3_CAP = 8 };

@@ -14,6 +14,11 @@
 // All kernels take a slot index (blockIdx.y) so that one launch serves a
 // batch of signals sharing a plan.  FP64 instantiations reproduce the CPU
 // definition bit for bit; FP32 ones accumulate in float.
+#include <algorithm>
+#include <cstdlib>
+#include <tuple>
+#include <mutex>
+#include <map>
 #include <cfloat>
 #include <climits>
 
@@ -401,6 +406,72 @@ __device__ __forceinline__ void sort_net(float (&v)[N]) {
   Cswap<N, 0, SortNet<N>::C>::run(v);
 }
 
+// The same network pruned to output M only (backward liveness): a
+// comparator whose outputs are both dead is dropped, one with a single
+// live output keeps only its min or its max.
+template <int N, int M>
+struct MedNet {
+  static constexpr int C = SortNet<N>::C;
+  signed char kind[C > 0 ? C : 1];  // 0 drop, 1 both, 2 min only, 3 max only
+  constexpr MedNet() : kind() {
+    bool live[N > 0 ? N : 1] = {};
+    live[M] = true;
+    for (int c = C - 1; c >= 0; c--) {
+      const int i = NetOf<N>::net.a[c], j = NetOf<N>::net.b[c];
+      const bool li = live[i], lj = live[j];
+      kind[c] = li && lj ? 1 : li ? 2 : lj ? 3 : 0;
+      if (li || lj) live[i] = live[j] = true;
+    }
+  }
+};
+template <int N, int M> struct MedOf { static constexpr MedNet<N, M> net{}; };
+
+template <int N, int M, int c, int C>
+struct Cmed {
+  static __device__ __forceinline__ void run(float (&v)[N]) {
+    constexpr int i = NetOf<N>::net.a[c], j = NetOf<N>::net.b[c];
+    constexpr int k = MedOf<N, M>::net.kind[c];
+    if constexpr (k == 1) {
+      const float x = v[i], y = v[j];
+      v[i] = fminf(x, y);
+      v[j] = fmaxf(x, y);
+    } else if constexpr (k == 2) {
+      v[i] = fminf(v[i], v[j]);
+    } else if constexpr (k == 3) {
+      v[j] = fmaxf(v[i], v[j]);
+    }
+    Cmed<N, M, c + 1, C>::run(v);
+  }
+};
+template <int N, int M, int C>
+struct Cmed<N, M, C, C> {
+  static __device__ __forceinline__ void run(float (&)[N]) {}
+};
+
+// Element M of v in sorted order (v is overwritten).
+template <int N, int M>
+__device__ __forceinline__ float select_net(float (&v)[N]) {
+  Cmed<N, M, 0, SortNet<N>::C>::run(v);
+  return v[M];
+}
+
+// Lower median of v[0..Lr): the pruned network when Lr == LN is known at
+// compile time, else a full sort (v is overwritten).
+template <int LN, bool EXACT>
+__device__ __forceinline__ float lower_median(float (&v)[LN], int Lr) {
+  if constexpr (EXACT) {
+    return select_net<LN, (LN - 1) / 2>(v);
+  } else {
+    sort_net(v);
+    const int m = (Lr - 1) >> 1;
+    float r = 0;
+#pragma unroll
+    for (int j = 0; j < LN; j++)
+      if (j == m) r = v[j];
+    return r;
+  }
+}
+
 __device__ __forceinline__ long long okey(double v) {
   long long b = __double_as_longlong(v);
   return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
@@ -425,7 +496,8 @@ __device__ __forceinline__ Slot loop_slot(const V12Dev &d, int j) {
 // (computefourier-1.0-2.0.cc:370-378)
 __device__ __forceinline__ void bucket_of(const V12Dev &d, const Slot &s, unsigned f, unsigned long long ai,
                                           int &hashed, int &m) {
-  const unsigned long long p = ((unsigned long long)f * ai) & ((unsigned long long)d.n - 1);
+  // n is a power of two below 2^32: the product's low bits suffice
+  const unsigned p = (f * (unsigned)ai) & ((unsigned)d.n - 1u);
   hashed = (int)(p >> s.lq);
   int dist = (int)(p & (s.q - 1));
   if (dist > (s.q >> 1)) {
@@ -493,44 +565,54 @@ __device__ __noinline__ double2 median64_exact(const V12Dev &d, const double2 *x
   return make_double2(mre, mim);
 }
 
-// Candidate h of a slot: v1 hits, v2 every comb candidate.  Returns false
-// when h is past the end; publishes the count once.
-__device__ __forceinline__ bool candidate(const V12Dev &d, int slot, long h, unsigned &f) {
+// Number of candidates of a slot: v1 hits, v2 every comb candidate.
+__device__ __forceinline__ long cand_total(const V12Dev &d, int slot) {
+  const int *cnt = d.counters + slot * CNT_STRIDE;
+  if (d.version == 0) return min(cnt[CNT_HITS], d.hit_cap);
+  return (long)cnt[CNT_COMB] * (d.n / d.W);
+}
+
+// Frequency of candidate h (< cand_total) of a slot.  v2 candidates are
+// numbered residue-major, h = residue index * (n / W) + repetition, so the
+// lanes of a warp share a comb residue: for each loop their window index
+// (which depends on the residue only when the window length n / B divides
+// W) is one broadcast load.  The output is a set; its order is free.
+__device__ __forceinline__ unsigned cand_freq(const V12Dev &d, int slot, long h) {
+  if (d.version == 0) return (unsigned)d.hits[(long)slot * d.hit_cap + h];
+  const unsigned reps = (unsigned)(d.n / d.W);  // a power of two
+  const unsigned hu = (unsigned)h, ridx = hu >> (__ffs(reps) - 1), rep = hu & (reps - 1);
+  return rep * (unsigned)d.W + (unsigned)d.comb_list[(long)slot * d.W + ridx];
+}
+
+// Publishes a slot's output count (and the overflow flag).
+__device__ __forceinline__ void publish_count(const V12Dev &d, int slot, long total) {
   int *cnt = d.counters + slot * CNT_STRIDE;
-  long total;
-  if (d.version == 0) {
-    total = min(cnt[CNT_HITS], d.hit_cap);
-    if (h >= total) return false;
-    f = (unsigned)d.hits[(long)slot * d.hit_cap + h];
-  } else {
-    const int nc = cnt[CNT_COMB];
-    total = (long)nc * (d.n / d.W);
-    if (h >= total) return false;
-    const long rep = h / nc;
-    f = (unsigned)(rep * d.W + d.comb_list[(long)slot * d.W + (h - rep * nc)]);
-  }
-  if (h == 0) {
-    cnt[CNT_OUT] = (int)min(total, (long)d.out_cap);
-    if (d.out_count) d.out_count[slot] = (int)min(total, (long)d.out_cap);
-    if (total > d.out_cap) atomicOr(&cnt[CNT_ERR], ERR_OUT_OVERFLOW);
-  }
-  return h < d.out_cap;
+  const int c = (int)min(total, (long)d.out_cap);
+  cnt[CNT_OUT] = c;
+  if (d.out_count) d.out_count[slot] = c;
+  if (total > d.out_cap) atomicOr(&cnt[CNT_ERR], ERR_OUT_OVERFLOW);
+}
+
+// Candidate h of a slot; false when h is past the end.  Thread h == 0
+// publishes the count.
+__device__ __forceinline__ bool candidate(const V12Dev &d, int slot, long h, unsigned &f) {
+  const long total = cand_total(d, slot);
+  if (h == 0) publish_count(d, slot, total);
+  if (h >= total || h >= d.out_cap) return false;
+  f = cand_freq(d, slot, h);
+  return true;
 }
 
 // Picks the lower-median element of v[0..Lr) (FP32 approximations whose
 // exact values lie within +-e); returns its index if it is provably the
 // exact median, else -1.
-template <int LN>
+template <int LN, bool EXACT>
 __device__ __forceinline__ int proven_median(const float (&v)[LN], int Lr, float e) {
   float s[LN];
 #pragma unroll
   for (int j = 0; j < LN; j++) s[j] = v[j];
-  sort_net(s);
   const int m = (Lr - 1) >> 1;
-  float med = 0;
-#pragma unroll
-  for (int j = 0; j < LN; j++)
-    if (j == m) med = s[j];
+  const float med = lower_median<LN, EXACT>(s, Lr);
   int idx = -1;
 #pragma unroll
   for (int j = LN - 1; j >= 0; j--)
@@ -546,41 +628,88 @@ __device__ __forceinline__ int proven_median(const float (&v)[LN], int Lr, float
   return (below == m && above == Lr - 1 - m) ? idx : -1;
 }
 
-// FP32 form: values and medians in FP32.
-template <int LN, bool EXACT>
-__global__ void __launch_bounds__(128) k_estimate32(V12Dev d) {
-  const int slot = blockIdx.y;
-  const long h = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const float2 *wl = (const float2 *)d.win_loc, *we = (const float2 *)d.win_est;
-  unsigned f;
-  if (!candidate(d, slot, h, f)) return;
-  const int Lr = EXACT ? LN : d.L;
-  const int *rp = d.rparams + (long)slot * d.rp_stride;
-  const float2 *xs = (const float2 *)d.xs + (long)slot * d.xs_size;
-  float re[LN], im[LN];
-#pragma unroll
-  for (int j = 0; j < LN; j++) {
-    if (EXACT || j < Lr) {
-      float sc;
-      value32(d, xs, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
-    } else {
-      re[j] = INFINITY;
-      im[j] = INFINITY;
+// Estimation work is dealt in chunks of one candidate per thread from a
+// per-slot queue (counters[CNT_EST]).  A block starts on the slot its SM is
+// assigned (%smid modulo the slot count) and moves on only when that slot
+// is exhausted, so the blocks resident on one SM read one slot's bucket
+// array and its random lookups hit in L1 far more often than when an SM
+// serves several slots at once.
+__device__ __forceinline__ unsigned sm_id() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
+
+struct EstChunk {
+  int slot;
+  long base, end;
+};
+
+__device__ __forceinline__ bool next_chunk(const V12Dev &d, int nslots, int chunk, int &slot, int &visited,
+                                           EstChunk &out) {
+  __shared__ EstChunk sc;
+  __syncthreads();  // the previous chunk is read by every thread
+  if (threadIdx.x == 0) {
+    sc.base = -1;
+    while (visited < nslots) {
+      const long total = min(cand_total(d, slot), (long)d.out_cap);
+      const long c = (long)atomicAdd(&d.counters[slot * CNT_STRIDE + CNT_EST], 1) * chunk;
+      if (c < total) {
+        sc.slot = slot;
+        sc.base = c;
+        sc.end = min(c + chunk, total);
+        break;
+      }
+      slot = slot + 1 == nslots ? 0 : slot + 1;
+      visited++;
     }
   }
-  sort_net(re);
-  sort_net(im);
-  const int m = (Lr - 1) >> 1;
-  float mre = 0, mim = 0;
+  __syncthreads();
+  out = sc;
+  return out.base >= 0;
+}
+
+__device__ __forceinline__ void publish_all(const V12Dev &d, int nslots) {
+  if (blockIdx.x == 0)
+    for (int sl = threadIdx.x; sl < nslots; sl += blockDim.x) publish_count(d, sl, cand_total(d, sl));
+}
+
+// Resident 128-thread blocks per SM the estimation kernels are compiled
+// for (registers per thread = 65536 / (128 * blocks), without spills).
+constexpr int est32_blocks(int LN) { return LN <= 18 ? 8 : LN <= 24 ? 6 : 5; }
+constexpr int est64_blocks(int LN) { return LN <= 14 ? 6 : LN <= 24 ? 5 : 4; }
+
+// FP32 form: values and medians in FP32.
+template <int LN, bool EXACT>
+__global__ void __launch_bounds__(128, est32_blocks(LN)) k_estimate32(V12Dev d, int nslots) {
+  publish_all(d, nslots);
+  const float2 *wl = (const float2 *)d.win_loc, *we = (const float2 *)d.win_est;
+  const int Lr = EXACT ? LN : d.L;
+  int slot = (int)(sm_id() % (unsigned)nslots), visited = 0;
+  EstChunk ck;
+  while (next_chunk(d, nslots, blockDim.x, slot, visited, ck)) {
+    const int *rp = d.rparams + (long)ck.slot * d.rp_stride;
+    const float2 *xs = (const float2 *)d.xs + (long)ck.slot * d.xs_size;
+    const long h = ck.base + threadIdx.x;  // one candidate per thread and chunk
+    if (h < ck.end) {
+      const unsigned f = cand_freq(d, ck.slot, h);
+      float re[LN], im[LN];
 #pragma unroll
-  for (int j = 0; j < LN; j++)
-    if (j == m) {
-      mre = re[j];
-      mim = im[j];
+      for (int j = 0; j < LN; j++) {
+        if (EXACT || j < Lr) {
+          float sc;
+          value32(d, xs, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
+        } else {
+          re[j] = INFINITY;
+          im[j] = INFINITY;
+        }
+      }
+      const float mre = lower_median<LN, EXACT>(re, Lr), mim = lower_median<LN, EXACT>(im, Lr);
+      const long o = (long)ck.slot * d.out_stride + h;
+      d.out_idx[o] = (int)f;
+      ((float2 *)d.out_val)[o] = make_float2(mre, mim);
     }
-  const long o = (long)slot * d.out_stride + h;
-  d.out_idx[o] = (int)f;
-  ((float2 *)d.out_val)[o] = make_float2(mre, mim);
+  }
 }
 
 // FP64 form, bit-exact: the median element is chosen on FP32 copies with a
@@ -588,44 +717,49 @@ __global__ void __launch_bounds__(128) k_estimate32(V12Dev d) {
 // reference's exact operation sequence); anything not provable (ties,
 // near-ties) takes the all-exact path.
 template <int LN, bool EXACT>
-__global__ void __launch_bounds__(128) k_estimate64(V12Dev d) {
-  const int slot = blockIdx.y;
-  const long h = (long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(128, est64_blocks(LN)) k_estimate64(V12Dev d, int nslots) {
+  publish_all(d, nslots);
   const float2 *wl = (const float2 *)d.win32_loc, *we = (const float2 *)d.win32_est;
-  unsigned f;
-  if (!candidate(d, slot, h, f)) return;
   const int Lr = EXACT ? LN : d.L;
-  const int *rp = d.rparams + (long)slot * d.rp_stride;
-  const float2 *xs32 = (const float2 *)d.xs32 + (long)slot * d.xs_size;
-  const double2 *xs = (const double2 *)d.xs + (long)slot * d.xs_size;
-  float re[LN], im[LN];
-  float smax = 0.f;
+  int slot = (int)(sm_id() % (unsigned)nslots), visited = 0;
+  EstChunk ck;
+  while (next_chunk(d, nslots, blockDim.x, slot, visited, ck)) {
+    const int *rp = d.rparams + (long)ck.slot * d.rp_stride;
+    const float2 *xs32 = (const float2 *)d.xs32 + (long)ck.slot * d.xs_size;
+    const double2 *xs = (const double2 *)d.xs + (long)ck.slot * d.xs_size;
+    const long h = ck.base + threadIdx.x;  // one candidate per thread and chunk
+    if (h < ck.end) {
+      const unsigned f = cand_freq(d, ck.slot, h);
+      float re[LN], im[LN];
+      float smax = 0.f;
 #pragma unroll
-  for (int j = 0; j < LN; j++) {
-    if (EXACT || j < Lr) {
-      float sc;
-      value32(d, xs32, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
-      smax = fmaxf(smax, sc);
-    } else {
-      re[j] = INFINITY;
-      im[j] = INFINITY;
+      for (int j = 0; j < LN; j++) {
+        if (EXACT || j < Lr) {
+          float sc;
+          value32(d, xs32, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
+          smax = fmaxf(smax, sc);
+        } else {
+          re[j] = INFINITY;
+          im[j] = INFINITY;
+        }
+      }
+      // |exact - approx| <= 2^-20 * scale: each FP32 operand carries one
+      // rounding (2^-24 relative), plus two products and a sum; 4x margin.
+      const float e = smax * 0x1p-20f + 1e-30f;
+      const int ir = proven_median<LN, EXACT>(re, Lr, e);
+      const int ii = proven_median<LN, EXACT>(im, Lr, e);
+      double2 res;
+      if (ir >= 0 && ii >= 0) {
+        res.x = value64(d, xs, ir, f, (unsigned)rp[d.L + ir]).x;
+        res.y = value64(d, xs, ii, f, (unsigned)rp[d.L + ii]).y;
+      } else {
+        res = median64_exact(d, xs, rp, f);
+      }
+      const long o = (long)ck.slot * d.out_stride + h;
+      d.out_idx[o] = (int)f;
+      ((double2 *)d.out_val)[o] = res;
     }
   }
-  // |exact - approx| <= 2^-20 * scale: each FP32 operand carries one
-  // rounding (2^-24 relative), plus two products and a sum; 4x margin.
-  const float e = smax * 0x1p-20f + 1e-30f;
-  const int ir = proven_median<LN>(re, Lr, e);
-  const int ii = proven_median<LN>(im, Lr, e);
-  double2 res;
-  if (ir >= 0 && ii >= 0) {
-    res.x = value64(d, xs, ir, f, (unsigned)rp[d.L + ir]).x;
-    res.y = value64(d, xs, ii, f, (unsigned)rp[d.L + ii]).y;
-  } else {
-    res = median64_exact(d, xs, rp, f);
-  }
-  const long o = (long)slot * d.out_stride + h;
-  d.out_idx[o] = (int)f;
-  ((double2 *)d.out_val)[o] = res;
 }
 
 // ---------------------------------------------------------------- scatter --
@@ -701,38 +835,53 @@ static cudaError_t launch_bucket(const V12Dev &d, int nslots, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-#define SFFT_EST_KERNEL(NAME)                                                   \
+#define SFFT_EST_KERNEL(NAME, BLOCKS)                                           \
   template <int LN, bool EX>                                                    \
   struct NAME##_k {                                                             \
-    static void go(dim3 g, cudaStream_t s, const V12Dev &d) { NAME<LN, EX><<<g, 128, 0, s>>>(d); } \
+    static cudaError_t go(int nslots, cudaStream_t s, const V12Dev &d, int nsm) { \
+      NAME<LN, EX><<<nsm * BLOCKS(LN), 128, 0, s>>>(d, nslots);                 \
+      return cudaSuccess;                                                       \
+    }                                                                           \
   };
-SFFT_EST_KERNEL(k_estimate32)
-SFFT_EST_KERNEL(k_estimate64)
+SFFT_EST_KERNEL(k_estimate32, est32_blocks)
+SFFT_EST_KERNEL(k_estimate64, est64_blocks)
 #undef SFFT_EST_KERNEL
 
 template <template <int, bool> class KS>
-static cudaError_t dispatch_estimate(const V12Dev &d, dim3 grid, cudaStream_t s) {
+static cudaError_t dispatch_estimate(const V12Dev &d, int nslots, int nsm, cudaStream_t s) {
+  cudaError_t e;
   switch (d.L) {
-#define SFFT_L(v) \
-  case v:         \
-    KS<v, true>::go(grid, s, d); \
+#define SFFT_L(v)                                             \
+  case v:                                                     \
+    if ((e = KS<v, true>::go(nslots, s, d, nsm))) return e; \
     break;
     SFFT_L(8) SFFT_L(9) SFFT_L(10) SFFT_L(11) SFFT_L(12) SFFT_L(13) SFFT_L(14) SFFT_L(15) SFFT_L(16)
     SFFT_L(17) SFFT_L(18) SFFT_L(19) SFFT_L(20) SFFT_L(21) SFFT_L(22) SFFT_L(23) SFFT_L(24)
 #undef SFFT_L
     default:
       if (d.L > 32) return cudaErrorInvalidValue;
-      KS<32, false>::go(grid, s, d);
+      if ((e = KS<32, false>::go(nslots, s, d, nsm))) return e;
   }
   return cudaGetLastError();
 }
 
+// Multiprocessor count of the current device (cached per device).
+static int sm_count() {
+  static int cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cache[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+    cache[dev] = v;
+  }
+  return cache[dev];
+}
+
 template <typename R>
 static cudaError_t launch_estimate(const V12Dev &d, int nslots, cudaStream_t s) {
-  const int cap = d.version == 0 ? d.hit_cap : d.out_cap;
-  dim3 grid((cap + 127) / 128, nslots);
-  if (sizeof(R) == 8) return dispatch_estimate<k_estimate64_k>(d, grid, s);
-  return dispatch_estimate<k_estimate32_k>(d, grid, s);
+  if (sizeof(R) == 8) return dispatch_estimate<k_estimate64_k>(d, nslots, sm_count(), s);
+  return dispatch_estimate<k_estimate32_k>(d, nslots, sm_count(), s);
 }
 
 template <typename R, typename In>
