@@ -45,8 +45,9 @@ def args_():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--pool", type=int, default=64)
-    ap.add_argument("--only", default="all", choices=["all", "device"],
-                    help="device: only the device-resident timed legs (for profiler captures)")
+    ap.add_argument("--only", default="all", choices=["all", "device", "uneven"],
+                    help="device: only the device-resident timed legs (for profiler captures); "
+                         "uneven: only the 256-signal uneven batch")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -264,6 +265,12 @@ def gb300_arm(a, ws, rank, local):
             stages = (list(ms)[:4], cnt)
         return total, per, launches, stages
 
+    if a.only == "uneven":
+        if rank == 0:
+            print(json.dumps({"uneven_batch": uneven_leg(L, _lib, local),
+                              "uneven_batch_fp64": uneven_leg(L, _lib, local, precision=0)}), flush=True)
+        return
+
     # ---- FP32 headline (clocks sampled during its timed region)
     with Clocks(local) as clk:
         t32, per32, launches32, st32 = timed(p32, oval32, a.steps, a.warmup, profile=True)
@@ -311,6 +318,9 @@ def gb300_arm(a, ws, rank, local):
     # ---- e2e through the drop-in call with page-locked host buffers
     e2e = e2e_leg(L, p32, pool, B, a)
 
+    # ---- 256 signals of uneven (n, k) as one CUDA graph
+    uneven = uneven_leg(L, _lib, local)
+
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": t32max / a.steps, "higher_is_better": True, "scaling": "weak",
@@ -333,6 +343,7 @@ def gb300_arm(a, ws, rank, local):
         "stage_ms_per_launch_fp32": stage_table(st32),
         "stage_ms_per_launch_fp64": stage_table(st64),
         "e2e": e2e,
+        "uneven_batch": uneven,
         "gpu_launches": launches32,
         "clocks": clocks,
     }
@@ -344,6 +355,92 @@ def gb300_arm(a, ws, rank, local):
                                           "OpenMP over signals"}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def uneven_shapes(count=256):
+    """(n, k) of the uneven batch: n log-uniform over 2^16..2^22, k uniform
+    in [10, 500], drawn from seed s for signal s."""
+    out = []
+    for s in range(count):
+        r = np.random.default_rng(s)
+        out.append((1 << int(r.integers(16, 23)), int(r.integers(10, 501))))
+    return out
+
+
+def uneven_leg(L, _lib, local, steps=20, warmup=3, precision=1):
+    """256 v2 signals of uneven (n, k) (k-sparse, magnitude 1, 40 dB SNR,
+    seeds 0..255) through sfft_mixed_*: autotuned constants per (n, k
+    bucket), every plan's batched pipeline a branch of one CUDA graph that is
+    replayed per call."""
+    import torch
+    from sfft_gb300 import signals
+    shapes = uneven_shapes()
+    num = len(shapes)
+    sigs = [signals.make_signal_torch(n, k, s, snr_db=40.0, device=torch.device("cuda", local))
+            for s, (n, k) in enumerate(shapes)]
+    torch.cuda.synchronize()
+    arr = lambda vals: (ctypes.c_int * num)(*vals)
+    t0 = time.perf_counter()
+    m = L.sfft_mixed_create(num, arr([n for n, _ in shapes]), arr([k for _, k in shapes]), arr([1] * num),
+                            arr([precision] * num), 0, 2, local)
+    if not m:
+        return {"error": _lib_err(L)}
+    ins = (ctypes.c_void_p * num)(*[x.data_ptr() for x, _, _ in sigs])
+    seeds = (ctypes.c_uint * num)(*range(num))
+
+    def run():
+        if L.sfft_mixed_exec(m, ins, seeds) != 0:
+            raise RuntimeError(_lib_err(L))
+
+    run()
+    if L.sfft_mixed_sync(m) != 0:
+        raise RuntimeError(_lib_err(L))
+    setup = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(L.sfft_mixed_stream(m))
+    for _ in range(warmup):
+        run()
+    L.sfft_mixed_sync(m)
+    launches0 = L.sfft_kernel_launches()
+    dev, wall = [], []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        e1.synchronize()
+        wall.append(time.perf_counter() - w0)
+        dev.append(e0.elapsed_time(e1) * 1e-3)
+    L.sfft_mixed_sync(m)
+    # accuracy of the last call against the drawn spectra
+    missed = spurious = 0
+    worst, l1 = 0.0, []
+    for s, (x, pos, vals) in enumerate(sigs):
+        n = shapes[s][0]
+        c = L.sfft_mixed_result_host(m, s, None, None, 0)
+        hi = np.empty(max(c, 1), dtype=np.int32)
+        hv = np.empty(max(c, 1), dtype=np.complex64 if precision else np.complex128)
+        if L.sfft_mixed_result_host(m, s, hi.ctypes.data, hv.ctypes.data, c) != c:
+            raise RuntimeError(_lib_err(L))
+        est = np.zeros(n, dtype=np.complex128)
+        est[hi[:c]] = np.conj(hv[:c].astype(np.complex128))
+        err = np.abs(est[pos] - vals)
+        worst = max(worst, float(err.max(initial=0.0)))
+        l1.append(float(err.mean()))
+        missed += int(np.count_nonzero(err > 0.5))
+        est[pos] = 0
+        spurious += int(np.count_nonzero(np.abs(est) > 0.5))
+    groups = L.sfft_mixed_groups(m)
+    L.sfft_mixed_destroy(m)
+    return {"signals": num, "plans": groups, "precision": "fp32" if precision else "fp64",
+            "solves_per_s": num / float(np.median(dev)), "ms_per_call": 1e3 * float(np.median(dev)),
+            "ms_per_call_p99": 1e3 * pct(dev, 99),
+            "wall_solves_per_s": num / float(np.median(wall)),
+            "setup_s": setup, "kernel_launches_per_call": (L.sfft_kernel_launches() - launches0) / steps,
+            "accuracy_vs_truth": {"missed": missed, "spurious": spurious, "worst_tone_error": worst,
+                                  "mean_l1_on_support": float(np.mean(l1))},
+            "workload": "256 v2 signals, n log-uniform 2^16..2^22, k uniform [10,500], |X|=1, 40 dB SNR, "
+                        "seeds 0..255; autotuned constants per (n, k bucket); one CUDA graph per call"}
 
 
 def serving_leg(L, _lib, pool, precision, rate, nreq, device):

@@ -210,8 +210,10 @@ struct sfft_server_options
   int device;                   /* CUDA device, -1 = current */
   int max_batch;                /* transforms per batch of one plan (0: 32) */
   long hbm_budget_bytes;        /* device memory for plans + batches (0: 80% of free) */
-  int k_round;                  /* 1: round k up to the grid ceil(8 * 2^(j/4)) */
-  int tune_invalid;             /* 1: v1/v2 (n, k) outside the reference's domain get tuned constants */
+  int k_round;                  /* 1: round k up to the grid ceil(8 * 2^(j/4)); 2: to a power of two */
+  int tune_invalid;             /* v1/v2: 1 shapes outside the reference's domain get tuned constants;
+                                   2 every v1/v2 request uses autotuned constants, k rounded to its bucket;
+                                   1 and 2: v3 requests with k < 8 run on the smallest v3 plan (k = 8) */
 };
 typedef struct sfft_server_options sfft_server_options;
 
@@ -236,12 +238,14 @@ int sfft_server_stats(sfft_server *s, long *stats, int nstats);
 
 /* sfft_exec_many for `num` signals whose (n[i], k[i], version[i],
  * precision[i]) may all differ (precision may be NULL: FP64).  Signals of
- * one shape share a plan and run batched; all groups run concurrently as
- * branches of one CUDA graph that later calls replay.  tune_invalid: v1/v2
- * shapes outside the reference's domain get tuned constants. */
+ * one plan share it and run batched; all groups run concurrently as
+ * branches of one CUDA graph that later calls replay.  tune (v1/v2 only):
+ * 0 the reference's constants; 1 those, else tuned constants for shapes
+ * outside the reference's domain; 2 autotuned constants per (n, k bucket),
+ * k rounded up to its bucket (sfft_tuned_k) so that nearby k share a plan. */
 typedef struct sfft_mixed sfft_mixed;
 sfft_mixed *sfft_mixed_create(int num, const int *n, const int *k, const int *version, const int *precision,
-                              int in_type, int tune_invalid, int device);
+                              int in_type, int tune, int device);
 /* One execution: in[i] device pointers; seeds (or NULL) as in
  * sfft_exec_batch_ex.  Asynchronous; sfft_mixed_sync waits. */
 int sfft_mixed_exec(sfft_mixed *m, const void *const *in, const unsigned *seeds);
@@ -249,8 +253,21 @@ int sfft_mixed_sync(sfft_mixed *m);
 /* Device pointers to signal s's result (indices, values of value_bytes =
  * 16 (complex128) or 8 (complex64) each, capacity); returns its count. */
 int sfft_mixed_result(sfft_mixed *m, int s, const int **idx, const void **val, int *value_bytes, long *cap);
+/* The same copied to host memory (at most cap entries; values as above).
+ * Returns the signal's count, or -1. */
+long sfft_mixed_result_host(sfft_mixed *m, int s, int *idx, void *val, long cap);
 int sfft_mixed_groups(const sfft_mixed *m);
+/* The stream (cudaStream_t) the batch's graph runs on. */
+void *sfft_mixed_stream(const sfft_mixed *m);
 void sfft_mixed_destroy(sfft_mixed *m);
+
+/* ---- constants chosen by this project (no counterpart in the reference) */
+
+/* v1/v2 constants for (n, k): the autotuner's table row for n and the k
+ * bucket of k (returns 1), else a rule (returns 0); -1 if neither applies. */
+int sfft_tuned_params(int n, int k, int version, sfft_params *params);
+/* The k bucket: the next power of two >= max(k, 16). */
+int sfft_tuned_k(int k);
 
 /* Host-only plan queries (no GPU needed): the parameters a plan for
  * (n, k, version) would use, as the reference computes them.  fields:
@@ -258,6 +275,10 @@ void sfft_mixed_destroy(sfft_mixed *m);
  * loops_thresh, loops_est, w_loc, w_est, x_samp_size; v3: W_Man, B_g1,
  * w_g1, B_g2, w_g2.  Returns the number of fields written, or -1. */
 int sfft_describe_plan(int n, int k, enum sfft_version version, long *fields, int nfields);
+/* The same for a v1/v2 plan with explicit constants (no counterpart in the
+ * reference). */
+int sfft_describe_plan_params(int n, int k, enum sfft_version version, const sfft_params *params, long *fields,
+                              int nfields);
 /* The filter a plan would use: which 0 = location / first Gaussian,
  * 1 = estimation / second Gaussian; time taps (2*w doubles) and the
  * n-point spectrum (2*n doubles, may be NULL).  Returns w, or -1. */

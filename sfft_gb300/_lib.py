@@ -108,6 +108,12 @@ def load(build_if_missing=False):
     L.sfft_server_submit.argtypes = [vp, ci, ci, ci, ci, vp, ci, ctypes.c_uint]
     L.sfft_server_wait.restype = cl
     L.sfft_server_wait.argtypes = [vp, cl, vp, vp, cl, ctypes.POINTER(ctypes.c_double)]
+    L.sfft_describe_plan_params.restype = ci
+    L.sfft_describe_plan_params.argtypes = [ci, ci, ci, ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_long), ci]
+    L.sfft_tuned_params.restype = ci
+    L.sfft_tuned_params.argtypes = [ci, ci, ci, ctypes.POINTER(Params)]
+    L.sfft_tuned_k.restype = ci
+    L.sfft_tuned_k.argtypes = [ci]
     L.sfft_mixed_create.restype = vp
     L.sfft_mixed_create.argtypes = [ci, vp, vp, vp, vp, ci, ci, ci]
     L.sfft_mixed_exec.restype = ci
@@ -117,9 +123,13 @@ def load(build_if_missing=False):
     L.sfft_mixed_result.restype = ci
     L.sfft_mixed_result.argtypes = [vp, ci, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(ci),
                                     ctypes.POINTER(cl)]
+    L.sfft_mixed_result_host.restype = cl
+    L.sfft_mixed_result_host.argtypes = [vp, ci, vp, vp, cl]
     L.sfft_mixed_groups.restype = ci
     L.sfft_mixed_groups.argtypes = [vp]
     L.sfft_mixed_destroy.argtypes = [vp]
+    L.sfft_mixed_stream.restype = vp
+    L.sfft_mixed_stream.argtypes = [vp]
     L.sfft_server_plan_bytes.restype = cl
     L.sfft_server_plan_bytes.argtypes = [ci, ci, ci, ci, ci]
     L.sfft_server_stats.restype = ci

@@ -24,8 +24,8 @@ CU_SOURCES = ["v12.cu", "v3.cu", "noalloc.cu"]
 # v3 reproduces the reference's phase arguments (up to ~1e12 rad), whose
 # last-ulp rounding matters: no multiply-add contraction in that file.
 CU_EXTRA = {"v3.cu": ["--fmad=false"]}
-CC_SOURCES = ["api.cc", "host_plan.cc", "serve.cc", "mixed.cc"]
-HEADERS = ["common.cuh", "engine.h", "host_plan.h"]
+CC_SOURCES = ["api.cc", "host_plan.cc", "serve.cc", "mixed.cc", "tune.cc"]
+HEADERS = ["common.cuh", "engine.h", "host_plan.h", "tuned_table.inc"]
 
 
 def _cuda_home():
@@ -70,7 +70,7 @@ def build(verbose=False, ptxas_info=False):
     for s in CC_SOURCES:
         src, obj = os.path.join(CSRC, s), os.path.join(OBJ, s + ".o")
         if _stale(obj, [src] + hdrs):
-            jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall",
+            jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-Wall",
                          "-Wno-unused-function", "-c", src, "-o", obj] + inc)
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         outs = list(ex.map(_run, jobs))
@@ -80,7 +80,7 @@ def build(verbose=False, ptxas_info=False):
                 print(o)
     objs = [os.path.join(OBJ, s + ".o") for s in CU_SOURCES + CC_SOURCES]
     if _stale(LIB, objs):
-        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lpthread"])
+        _run([nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lpthread", "-lgomp"])
     return LIB
 
 

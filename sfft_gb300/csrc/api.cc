@@ -128,7 +128,7 @@ struct PlanImpl {
   // workspace
   int slots = 0;
   DBuf xs, xs32, xs_tmp, comb_buf, comb_tmp, J, score, hits, comb_bits, comb_list, counters, out_idx, out_val;
-  DBuf man, g1, g2, perm, est_f, est_v, map_keys, map_vals, map_list;
+  DBuf man, man_tmp, g1, g2, perm, est_f, est_v, map_keys, map_vals, map_list;
   DBuf rparams, inputs, dense_ptrs, in_stage, dense_stage, trace;
   std::vector<unsigned> epoch;
   int hit_cap = 0, out_cap = 0, est_cap = 0, map_cap = 0, table_cap = 0;
@@ -195,6 +195,48 @@ bool upload_twiddles(DBuf &b, long N, int prec) {
   std::vector<double> t(tw.begin(), tw.begin() + 2 * N);
   if (prec == sfft::PREC_FP64) return b.upload(t);
   return b.upload(to_f32(t));
+}
+
+// Plan-time FFTs of power-of-two length n >= 2^15 on the plan's device.
+// The global-memory Stockham stages perform exactly host_fft's operations
+// (the backward transform conjugates on the host around a forward one), so
+// the filters built this way are bit-identical to the host's; on any CUDA
+// failure the host FFT runs instead.
+bool device_fft(long n, double *data, int sign, void *ctx) {
+  if (n < (1L << 15) || (n & (n - 1))) return false;
+  const int dev = *(const int *)ctx;
+  if (cudaSetDevice(dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const std::vector<double> &tw = sfft::fft_twiddles(n);
+  const size_t bytes = sizeof(double) * 2 * (size_t)n;
+  void *a = nullptr, *b = nullptr, *t = nullptr;
+  cudaStream_t s = nullptr;
+  auto conj = [&] {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; i++) data[2 * i + 1] = -data[2 * i + 1];
+  };
+  bool good = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&a, bytes) == cudaSuccess && cudaMalloc(&b, bytes) == cudaSuccess &&
+              cudaMalloc(&t, bytes) == cudaSuccess;
+  if (good) {
+    std::vector<double> out(2 * (size_t)n);  // data stays intact until success
+    if (sign > 0) conj();
+    good = cudaMemcpyAsync(a, data, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+           cudaMemcpyAsync(t, tw.data(), bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+           sfft::global_fft_c128(a, b, (int)n, 1, n, n, 1, t, s) == cudaSuccess &&
+           cudaMemcpyAsync(out.data(), a, bytes, cudaMemcpyDeviceToHost, s) == cudaSuccess;
+    good = cudaStreamSynchronize(s) == cudaSuccess && good;
+    if (good) std::memcpy(data, out.data(), bytes);
+    if (sign > 0) conj();
+  }
+  cudaGetLastError();
+  if (a) cudaFree(a);
+  if (b) cudaFree(b);
+  if (t) cudaFree(t);
+  if (s) cudaStreamDestroy(s);
+  return good;
 }
 
 // Estimation window of a v1/v2 filter: the q = n/B entries of filter.freq
@@ -287,6 +329,7 @@ bool ensure_slots(PlanImpl &P, int want) {
     while (P.table_cap < 2 * P.map_cap) P.table_cap <<= 1;
     P.out_cap = P.map_cap;
     if (!P.perm.ensure(16 * 2 * (size_t)(p.w_g2 + 2) * S)) return false;
+    if (p.W_Man > sfft::v3_max_smem_fft() && !P.man_tmp.ensure(64 * (size_t)p.W_Man * S)) return false;
     if (!P.man.ensure(32 * (size_t)p.W_Man * S) || !P.g1.ensure(32 * (size_t)p.B_g1 * S) ||
         !P.g2.ensure(32 * (size_t)p.B_g2 * S) || !P.est_f.ensure(sizeof(int) * P.est_cap * S) ||
         !P.est_v.ensure(16 * (size_t)P.est_cap * S) || !P.map_keys.ensure(sizeof(int) * P.table_cap * S) ||
@@ -451,6 +494,8 @@ sfft::V3Dev v3_view(PlanImpl &P) {
   d.tw_g1 = P.tw_a.p;
   d.tw_g2 = P.tw_b.p;
   d.man = P.man.p;
+  d.man_tmp = P.man_tmp.p;
+  d.large_man = p.W_Man > sfft::v3_max_smem_fft();
   d.g1 = P.g1.p;
   d.g2 = P.g2.p;
   d.perm = P.perm.p;
@@ -518,6 +563,7 @@ void shift_view(PlanImpl &P, sfft::V12Dev &d, int base, bool own_out) {
 void shift_view(PlanImpl &P, sfft::V3Dev &d, int base, bool own_out) {
   if (!base) return;
   shift(d.man, 32 * (size_t)d.W, base);
+  if (d.large_man) shift(d.man_tmp, 64 * (size_t)d.W, base);
   shift(d.g1, 32 * (size_t)d.B1, base);
   shift(d.g2, 32 * (size_t)d.B2, base);
   shift(d.perm, 16 * 2 * (size_t)(d.w2 + 2), base);
@@ -946,8 +992,11 @@ static sfft_plan *make_plan_impl(int n, int k, enum sfft_version version, const 
   cudaGetDevice(&P->device);
   std::string err;
   sfft::HostFilter fa, fb;
+  sfft::BuildOpts bo;
+  bo.fft = device_fft;
+  bo.ctx = &P->device;
   if (P->version < 2) {
-    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, P->version == 1, P->p12, fa, fb, err, knobs)) {
+    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, P->version == 1, P->p12, fa, fb, err, knobs, &bo)) {
       set_err(err);
       return nullptr;
     }
@@ -979,13 +1028,13 @@ static sfft_plan *make_plan_impl(int n, int k, enum sfft_version version, const 
         !upload_twiddles(P->tw_c, std::max(p.W_Comb, 2), P->prec))
       return nullptr;
   } else {
-    if (sfft::build_v3_plan((unsigned)n, (unsigned)k, P->p3, fa, fb, err)) {
+    if (sfft::build_v3_plan((unsigned)n, (unsigned)k, P->p3, fa, fb, err, &bo)) {
       set_err(err);
       return nullptr;
     }
     const auto &p = P->p3;
-    if (p.W_Man > 8192 || p.B_g1 > 8192) {
-      set_err("v3 comb wider than 8192 buckets is not supported by this build");
+    if (p.B_g1 > sfft::v3_max_smem_fft()) {
+      set_err("v3 with more than 8192 Gaussian buckets (k >= 8192) is not supported by this build");
       return nullptr;
     }
     P->win_half_a = 3 * (n / p.B_g1) / 2 + 2;
@@ -1062,7 +1111,7 @@ long sfft_plan_footprint(const sfft_plan *plan) {
   const DBuf *bufs[] = {&P->taps_a, &P->taps_b, &P->win_a, &P->win_b, &P->win32_a, &P->win32_b, &P->tw_a,
                         &P->tw_b, &P->tw_c, &P->xs, &P->xs32, &P->xs_tmp, &P->comb_buf, &P->comb_tmp, &P->J,
                         &P->score, &P->hits, &P->comb_bits, &P->comb_list, &P->counters, &P->out_idx,
-                        &P->out_val, &P->man, &P->g1, &P->g2, &P->perm, &P->est_f, &P->est_v, &P->map_keys,
+                        &P->out_val, &P->man, &P->man_tmp, &P->g1, &P->g2, &P->perm, &P->est_f, &P->est_v, &P->map_keys,
                         &P->map_vals, &P->map_list, &P->rparams, &P->inputs, &P->dense_ptrs, &P->in_stage,
                         &P->dense_stage, &P->trace};
   long total = 0;
@@ -1281,10 +1330,12 @@ int sfft_describe_plan(int n, int k, enum sfft_version version, long *fields, in
   }
   std::string err;
   sfft::HostFilter fa, fb;
+  sfft::BuildOpts bo;
+  bo.filters = false;  // parameters and tap counts only
   std::vector<long> v;
   if (version == SFFT_VERSION_1 || version == SFFT_VERSION_2) {
     sfft::V12Params p;
-    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, version == SFFT_VERSION_2, p, fa, fb, err)) {
+    if (sfft::build_v12_plan((unsigned)n, (unsigned)k, version == SFFT_VERSION_2, p, fa, fb, err, nullptr, &bo)) {
       set_err(err);
       return -1;
     }
@@ -1292,7 +1343,7 @@ int sfft_describe_plan(int n, int k, enum sfft_version version, long *fields, in
          p.w_loc, p.w_est, p.x_samp_size};
   } else if (version == SFFT_VERSION_3) {
     sfft::V3Params p;
-    if (sfft::build_v3_plan((unsigned)n, (unsigned)k, p, fa, fb, err)) {
+    if (sfft::build_v3_plan((unsigned)n, (unsigned)k, p, fa, fb, err, &bo)) {
       set_err(err);
       return -1;
     }
@@ -1302,6 +1353,41 @@ int sfft_describe_plan(int n, int k, enum sfft_version version, long *fields, in
     return -1;
   }
   const int m = std::min<int>(nfields, (int)v.size());
+  for (int i = 0; i < m; i++) fields[i] = v[i];
+  return m;
+}
+
+int sfft_describe_plan_params(int n, int k, enum sfft_version version, const sfft_params *params, long *fields,
+                              int nfields) {
+  if (!params) return sfft_describe_plan(n, k, version, fields, nfields);
+  g_err.clear();
+  if (!fields || n < 16 || (n & (n - 1)) || k < 1 || version == SFFT_VERSION_3) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  sfft::V12Knobs kn;
+  kn.set = true;
+  kn.Bcst_loc = params->Bcst_loc;
+  kn.Bcst_est = params->Bcst_est;
+  kn.Comb_cst = params->Comb_cst;
+  kn.loc_loops = params->loc_loops;
+  kn.est_loops = params->est_loops;
+  kn.threshold_loops = params->threshold_loops;
+  kn.comb_loops = params->comb_loops;
+  kn.tolerance_loc = params->tolerance_loc;
+  kn.tolerance_est = params->tolerance_est;
+  sfft::BuildOpts bo;
+  bo.filters = false;
+  sfft::V12Params p;
+  sfft::HostFilter fa, fb;
+  std::string err;
+  if (sfft::build_v12_plan((unsigned)n, (unsigned)k, version == SFFT_VERSION_2, p, fa, fb, err, &kn, &bo)) {
+    set_err(err);
+    return -1;
+  }
+  const long v[] = {p.B_loc,     p.B_thresh, p.B_est, p.W_Comb, p.Comb_loops,   p.loops_loc,
+                    p.loops_thresh, p.loops_est, p.w_loc, p.w_est, p.x_samp_size};
+  const int m = std::min<int>(nfields, 11);
   for (int i = 0; i < m; i++) fields[i] = v[i];
   return m;
 }

@@ -89,6 +89,8 @@ struct V3Dev {
   const void *tw_man, *tw_g1, *tw_g2;
   // per-slot workspace
   void *man;     // 2W complex (interleaved loops)
+  void *man_tmp; // large_man: 4W complex (two W-point arrays and their FFT scratch)
+  int large_man; // W above the shared-memory FFT: Mansour comb FFTs in global memory
   void *g1;      // 2*B1 complex
   void *g2;      // 2*B2 complex
   void *perm;    // (w2 + 1) complex
@@ -114,5 +116,12 @@ struct V3Dev {
 };
 
 cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t stream, StageEvents *se = nullptr);
+// Largest FP64 FFT the v3 filter kernel runs in shared memory.
+int v3_max_smem_fft();
+// Batched complex128 FFTs of length N in global memory (the same stages as
+// the shared-memory FFT): narr arrays per slot, arr_stride apart, slots
+// slot_stride apart; b is scratch of the same shape; result in a.
+cudaError_t global_fft_c128(void *a, void *b, int N, int narr, long arr_stride, long slot_stride, int nslots,
+                            const void *tw, cudaStream_t s);
 
 }  // namespace sfft

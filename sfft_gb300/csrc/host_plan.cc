@@ -55,6 +55,7 @@ static std::vector<double> make_twiddles(long N) {
     return tw;
   }
   const long Q = N / 4;
+#pragma omp parallel for schedule(static) if (Q >= (1 << 14))
   for (long u = 0; u < Q; u++) {
     const double a = (2.0 * M_PI * (double)u) / (double)N;
     const double c = std::cos(a), s = std::sin(a);
@@ -220,13 +221,21 @@ static void make_dolph_chebyshev(double lobefrac, double tolerance, HostFilter &
   for (int i = 0; i < w; i++) f.time[2 * i] = x[2 * ((i - r + w) % w)];
 }
 
+static void plan_fft(long n, double *data, int sign, const BuildOpts *opts) {
+  if (opts && opts->fft && opts->fft(n, data, sign, opts->ctx)) return;
+  host_fft(n, data, sign);
+}
+
 // src/filters.cc:109-160: flat-top "multiple" filter of width b over n.
-static void make_multiple(HostFilter &f, int n, int b) {
+// The running sums and the phase oscillator are sequential (their rounding
+// is part of the result); the magnitude maximum and the scaling are
+// elementwise and run in parallel.
+static void make_multiple(HostFilter &f, int n, int b, const BuildOpts *opts) {
   const int w = f.w;
   std::vector<double> g(2 * (size_t)n, 0.0);
   std::memcpy(g.data(), f.time.data() + 2 * (w / 2), sizeof(double) * 2 * (size_t)(w - w / 2));
   std::memcpy(g.data() + 2 * (size_t)(n - w / 2), f.time.data(), sizeof(double) * 2 * (size_t)(w / 2));
-  host_fft(n, g.data(), -1);
+  plan_fft(n, g.data(), -1, opts);
   double sr = 0, si = 0;
   for (int i = 0; i < b; i++) {
     sr += g[2 * i];
@@ -234,19 +243,23 @@ static void make_multiple(HostFilter &f, int n, int b) {
   }
   std::vector<double> &h = f.freq;
   h.assign(2 * (size_t)n, 0.0);
-  double mx = 0;
   const int offset = b / 2;
   for (long i = 0; i < n; i++) {
     const long d = (i + n + offset) % n;
     h[2 * d] = sr;
     h[2 * d + 1] = si;
-    const double m = std::hypot(sr, si);
-    mx = (mx < m) ? m : mx;
     const long ib = (i + b) % n;
     const double dr = g[2 * ib] - g[2 * i], di = g[2 * ib + 1] - g[2 * i + 1];
     sr = sr + dr;
     si = si + di;
   }
+  double mx = 0;
+#pragma omp parallel for reduction(max : mx) schedule(static) if (n >= (1 << 16))
+  for (long i = 0; i < n; i++) {
+    const double m = std::hypot(h[2 * i], h[2 * i + 1]);
+    mx = (mx < m) ? m : mx;
+  }
+#pragma omp parallel for schedule(static) if (n >= (1 << 16))
   for (long i = 0; i < n; i++) {
     h[2 * i] /= mx;
     h[2 * i + 1] /= mx;
@@ -264,7 +277,7 @@ static void make_multiple(HostFilter &f, int n, int b) {
     oci = ni;
   }
   std::memcpy(g.data(), h.data(), sizeof(double) * 2 * (size_t)n);
-  host_fft(n, g.data(), +1);
+  plan_fft(n, g.data(), +1, opts);
   for (int i = 0; i < w; i++) {
     f.time[2 * i] = g[2 * i] / n;
     f.time[2 * i + 1] = g[2 * i + 1] / n;
@@ -320,7 +333,7 @@ const Row *find_row(const Row (&t)[L], int key) {
 }  // namespace
 
 int build_v12_plan(unsigned n, unsigned k, bool comb, V12Params &p, HostFilter &loc,
-                   HostFilter &est, std::string &err, const V12Knobs *knobs) {
+                   HostFilter &est, std::string &err, const V12Knobs *knobs, const BuildOpts *opts) {
   double Bcst_loc = 1, Bcst_est = 1, Comb_cst = 2;
   int loc_loops = 4, est_loops = 16, threshold_loops = 3, comb_loops = 1;
   double tolerance_loc = 1.e-8, tolerance_est = 1.e-8;
@@ -380,8 +393,10 @@ int build_v12_plan(unsigned n, unsigned k, bool comb, V12Params &p, HostFilter &
     err = "filter wider than the signal";
     return -1;
   }
-  make_multiple(loc, (int)n, b_loc);
-  make_multiple(est, (int)n, b_est);
+  if (!opts || opts->filters) {
+    make_multiple(loc, (int)n, b_loc, opts);
+    make_multiple(est, (int)n, b_est, opts);
+  }
   p.w_loc = loc.w;
   p.w_est = est.w;
   p.x_samp_size = (long)p.loops_loc * p.B_loc + (long)p.loops_est * p.B_est;
@@ -389,7 +404,7 @@ int build_v12_plan(unsigned n, unsigned k, bool comb, V12Params &p, HostFilter &
 }
 
 int build_v3_plan(unsigned n, unsigned k, V3Params &p, HostFilter &g1, HostFilter &g2,
-                  std::string &err) {
+                  std::string &err, const BuildOpts *opts) {
   const double Bcst = 1, Bcst2 = 0.25, Mancst = 10;
   const double tolerance_g1 = 1.e-8, tolerance_g2 = 1.e-8;
   n = floor_to_pow2(n);
@@ -415,8 +430,10 @@ int build_v3_plan(unsigned n, unsigned k, V3Params &p, HostFilter &g1, HostFilte
     err = "filter wider than the signal";
     return -1;
   }
-  make_multiple(g1, (int)n, b_g1);
-  make_multiple(g2, (int)n, b_g2);
+  if (!opts || opts->filters) {
+    make_multiple(g1, (int)n, b_g1, opts);
+    make_multiple(g2, (int)n, b_g2, opts);
+  }
   p.w_g1 = g1.w;
   p.w_g2 = g2.w;
   return 0;

@@ -40,12 +40,24 @@ struct V12Knobs {
   double tolerance_loc = 1e-8, tolerance_est = 1e-8;
 };
 
+// How plan-time work is done.  `filters` false: only the parameters and
+// the filters' tap counts (the n-point filter spectra are skipped).  `fft`:
+// runs an n-point FFT of the same definition as host_fft (for instance on
+// the GPU the plan is for) and returns true, or returns false to leave it to
+// host_fft.
+struct BuildOpts {
+  bool filters = true;
+  bool (*fft)(long n, double *data, int sign, void *ctx) = nullptr;
+  void *ctx = nullptr;
+};
+
 // Returns 0, or -1 with `err` set when (n, k) is outside the domain on
 // which the reference's algorithm is defined.
 int build_v12_plan(unsigned n, unsigned k, bool comb, V12Params &p, HostFilter &loc,
-                   HostFilter &est, std::string &err, const V12Knobs *knobs = nullptr);
+                   HostFilter &est, std::string &err, const V12Knobs *knobs = nullptr,
+                   const BuildOpts *opts = nullptr);
 int build_v3_plan(unsigned n, unsigned k, V3Params &p, HostFilter &g1, HostFilter &g2,
-                  std::string &err);
+                  std::string &err, const BuildOpts *opts = nullptr);
 
 // The project's FFT (radix-4/2 Stockham + Bluestein); sign -1 forward,
 // +1 backward unnormalised.  data: n interleaved (re, im) doubles.

@@ -27,7 +27,8 @@ bool plan_enable_staging(sfft_plan *plan, int slots);
 bool plan_stage(sfft_plan *plan, int num, const void *const *in, const unsigned *seeds);
 bool plan_launch_staged(sfft_plan *plan, int num, int in_type, int *out_idx, void *out_val, int *out_count,
                         long stride, cudaStream_t s);
-bool tuned_params_for(int n, int k, sfft_params &p);
+int k_bucket(int k);
+sfft_plan *make_plan_tuned(int n, int k, int version, const sfft_options &o, int mode, bool &tuned);
 }  // namespace sfft
 
 namespace {
@@ -100,7 +101,7 @@ bool launch_all(sfft_mixed *m) {
 extern "C" {
 
 sfft_mixed *sfft_mixed_create(int num, const int *n, const int *k, const int *version, const int *precision,
-                              int in_type, int tune_invalid, int device) {
+                              int in_type, int tune, int device) {
   if (num < 1 || !n || !k || !version) {
     sfft::set_last_error("invalid arguments");
     return nullptr;
@@ -121,7 +122,9 @@ sfft_mixed *sfft_mixed_create(int num, const int *n, const int *k, const int *ve
   m->sig_slot.resize(num);
   for (int i = 0; i < num; i++) {
     const int v = version[i], pr = (v == SFFT_VERSION_3 || !precision) ? SFFT_PREC_FP64 : precision[i];
-    auto key = std::make_tuple(n[i], k[i], v, pr);
+    // mode 2: one plan per (n, k bucket)
+    const int kk = tune == 2 && v != SFFT_VERSION_3 ? sfft::k_bucket(k[i]) : k[i];
+    auto key = std::make_tuple(n[i], kk, v, pr);
     auto it = index.find(key);
     int gi;
     if (it == index.end()) {
@@ -129,7 +132,7 @@ sfft_mixed *sfft_mixed_create(int num, const int *n, const int *k, const int *ve
       index[key] = gi;
       Group g;
       g.n = n[i];
-      g.k = k[i];
+      g.k = kk;
       g.version = v;
       g.prec = pr;
       m->groups.push_back(g);
@@ -146,14 +149,7 @@ sfft_mixed *sfft_mixed_create(int num, const int *n, const int *k, const int *ve
   for (Group &g : m->groups) {
     const int cnt = (int)g.members.size();
     sfft_options o{g.prec, m->device, cnt};
-    g.plan = sfft_make_plan_ex(g.n, g.k, (enum sfft_version)g.version, FFTW_ESTIMATE, &o);
-    if (!g.plan && tune_invalid && g.version < 2) {
-      sfft_params p;
-      if (sfft::tuned_params_for(g.n, g.k, p)) {
-        g.plan = sfft_make_plan_params(g.n, g.k, (enum sfft_version)g.version, &p, &o);
-        g.tuned = g.plan != nullptr;
-      }
-    }
+    g.plan = sfft::make_plan_tuned(g.n, g.k, g.version, o, tune, g.tuned);
     if (!g.plan || !sfft::plan_enable_staging(g.plan, cnt)) {
       good = false;
       break;
@@ -230,7 +226,23 @@ int sfft_mixed_result(sfft_mixed *m, int s, const int **idx, const void **val, i
   return c;
 }
 
+long sfft_mixed_result_host(sfft_mixed *m, int s, int *idx, void *val, long cap) {
+  const int *di = nullptr;
+  const void *dv = nullptr;
+  int vb = 0;
+  long dcap = 0;
+  const int c = sfft_mixed_result(m, s, &di, &dv, &vb, &dcap);
+  if (c < 0) return -1;
+  const long n = std::min<long>(c, cap);
+  if (n > 0 && ((idx && !ok(cudaMemcpy(idx, di, sizeof(int) * n, cudaMemcpyDeviceToHost), "copy")) ||
+                (val && !ok(cudaMemcpy(val, dv, (size_t)vb * n, cudaMemcpyDeviceToHost), "copy"))))
+    return -1;
+  return c;
+}
+
 int sfft_mixed_groups(const sfft_mixed *m) { return m ? (int)m->groups.size() : -1; }
+
+void *sfft_mixed_stream(const sfft_mixed *m) { return m ? (void *)m->master : nullptr; }
 
 void sfft_mixed_destroy(sfft_mixed *m) {
   if (!m) return;

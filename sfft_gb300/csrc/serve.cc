@@ -35,6 +35,8 @@
 
 namespace sfft {
 void set_last_error(const char *m);
+int k_bucket(int k);
+sfft_plan *make_plan_tuned(int n, int k, int version, const sfft_options &o, int mode, bool &tuned);
 }
 
 namespace {
@@ -128,29 +130,16 @@ void host_done(void *arg) {
 
 int round_k(int k, int mode) {
   if (!mode || k <= 8) return k;
+  if (mode == 2) {
+    int b = 8;
+    while (b < k) b *= 2;
+    return b;
+  }
   // smallest value of the grid ceil(8 * 2^(j/4)) that is >= k
   for (int j = 0;; j++) {
     const int v = (int)std::ceil(8.0 * std::pow(2.0, j / 4.0));
     if (v >= k) return v;
   }
-}
-
-// Constants for (n, k) where the reference's own parameters leave fewer
-// than 2k+1 buckets: bucket counts and comb width of at least 4k.
-bool tuned_params(int n, int k, sfft_params &p) {
-  const double s = std::sqrt((double)n * k / std::log2((double)n));
-  if (8.0 * k > n / 2) return false;
-  p.Bcst_loc = p.Bcst_est = 8.0 * k / s;
-  int B = 1;
-  while (B * 2 <= p.Bcst_loc * s) B *= 2;
-  p.Comb_cst = std::max(2.0, 8.0 * k * B / (double)n);
-  p.loc_loops = 4;
-  p.est_loops = 16;
-  p.threshold_loops = 3;
-  p.comb_loops = 1;
-  p.tolerance_loc = 1e-8;
-  p.tolerance_est = 1e-8;
-  return true;
 }
 
 long device_free() {
@@ -179,9 +168,15 @@ bool make_room(sfft_server *s, long need) {
 }
 
 // Device bytes of a plan with `slots` batch slots, from its shape.
-long estimate_bytes(const PlanKey &key, int slots) {
+long estimate_bytes(const PlanKey &key, int slots, int tune) {
   long f[11];
-  const int m = sfft_describe_plan(key.n, key.k, (enum sfft_version)key.version, f, 11);
+  int m = -1;
+  sfft_params prm;
+  if (key.version < 2 && tune == 2 && sfft_tuned_params(key.n, key.k, key.version, &prm) >= 0)
+    m = sfft_describe_plan_params(key.n, key.k, (enum sfft_version)key.version, &prm, f, 11);
+  if (m < 0) m = sfft_describe_plan(key.n, key.k, (enum sfft_version)key.version, f, 11);
+  if (m < 0 && key.version < 2 && tune && sfft_tuned_params(key.n, key.k, key.version, &prm) >= 0)
+    m = sfft_describe_plan_params(key.n, key.k, (enum sfft_version)key.version, &prm, f, 11);
   const long cs = key.prec == SFFT_PREC_FP64 ? 16 : 8;
   if (m < 0) return 4L * key.n * 16 * slots;
   if (key.version < 2) {
@@ -199,22 +194,15 @@ long estimate_bytes(const PlanKey &key, int slots) {
 PlanEntry *get_plan(sfft_server *s, const PlanKey &key, std::string &err) {
   auto it = s->plans.find(key);
   if (it != s->plans.end()) return it->second;
-  const long need = estimate_bytes(key, s->max_batch);
+  const long need = estimate_bytes(key, s->max_batch, s->tune_invalid);
   if (need > s->budget) {
     err = "request needs more device memory than the server's budget";
     return nullptr;
   }
   if (!make_room(s, need)) return (PlanEntry *)-1;  // defer
   sfft_options o{key.prec, s->device, s->max_batch};
-  sfft_plan *p = sfft_make_plan_ex(key.n, key.k, (enum sfft_version)key.version, FFTW_ESTIMATE, &o);
   bool tuned = false;
-  if (!p && s->tune_invalid && key.version < 2) {
-    sfft_params prm;
-    if (tuned_params(key.n, key.k, prm)) {
-      p = sfft_make_plan_params(key.n, key.k, (enum sfft_version)key.version, &prm, &o);
-      tuned = p != nullptr;
-    }
-  }
+  sfft_plan *p = sfft::make_plan_tuned(key.n, key.k, key.version, o, s->tune_invalid, tuned);
   if (!p) {
     err = sfft_last_error();
     return nullptr;
@@ -390,7 +378,8 @@ long sfft_server_submit(sfft_server *s, int n, int k, enum sfft_version version,
   cudaGetLastError();
   Request *r = new Request();
   r->n = n;
-  r->k = round_k(k, s->k_round);
+  r->k = s->tune_invalid == 2 && version != SFFT_VERSION_3 ? sfft::k_bucket(k) : round_k(k, s->k_round);
+  if (s->tune_invalid && version == SFFT_VERSION_3 && r->k < 8) r->k = 8;
   r->version = (int)version;
   r->prec = version == SFFT_VERSION_3 ? SFFT_PREC_FP64 : precision;
   r->in = in;
@@ -467,7 +456,7 @@ long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val,
 long sfft_server_plan_bytes(int n, int k, enum sfft_version version, int precision, int max_batch) {
   if (n < 16 || (n & (n - 1)) || k < 1 || max_batch < 1) return -1;
   const int prec = version == SFFT_VERSION_3 ? SFFT_PREC_FP64 : precision;
-  return estimate_bytes(PlanKey{n, k, (int)version, prec}, max_batch);
+  return estimate_bytes(PlanKey{n, k, (int)version, prec}, max_batch, 0);
 }
 
 int sfft_server_stats(sfft_server *s, long *stats, int nstats) {
@@ -482,6 +471,3 @@ int sfft_server_stats(sfft_server *s, long *stats, int nstats) {
 
 }  // extern "C"
 
-namespace sfft {
-bool tuned_params_for(int n, int k, sfft_params &p) { return tuned_params(n, k, p); }
-}  // namespace sfft

@@ -939,6 +939,12 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
   return cudaSuccess;
 }
 
+cudaError_t global_fft_c128(void *a, void *b, int N, int narr, long arr_stride, long slot_stride, int nslots,
+                            const void *tw, cudaStream_t s) {
+  return global_fft<double>((double2 *)a, (double2 *)b, N, narr, arr_stride, slot_stride, nslots, (const double2 *)tw,
+                            s);
+}
+
 cudaError_t v12_run(const V12Dev &d, int nslots, cudaStream_t s, StageEvents *se) {
   if (d.prec == PREC_FP64)
     return d.in_type == IN_C128 ? run_typed<double, double2>(d, nslots, s, se)

@@ -30,10 +30,10 @@ __device__ __forceinline__ double2 ld_x(const void *base, int in_type, long i) {
 // --------------------------------------------------------------- filters --
 
 template <int PER>
-__global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d) {
+__global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d, int role0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2 *buf = (double2 *)smem_raw;
-  const int role = blockIdx.x, slot = blockIdx.y, l = role & 1;
+  const int role = blockIdx.x + role0, slot = blockIdx.y, l = role & 1;
   const int *rp = d.rparams + (long)slot * d.rp_stride;
   const unsigned long long mask = (unsigned long long)d.n - 1;
   const void *x = d.inputs[slot];
@@ -102,6 +102,28 @@ __global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d) {
   block_fft<double, PER>(buf, N, 31 - __clz(N), tw);
   for (int i = threadIdx.x; i < N; i += blockDim.x) dst[2 * i + l] = buf[i];
 }
+
+// Mansour comb of width W above the shared-memory FFT: the two samplings go
+// to contiguous arrays (man_tmp[slot][l][i]), are transformed by the
+// global-memory FFT, and are interleaved into man[slot][2 i + l].
+__global__ void k_v3_man_gather(V3Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, l = blockIdx.y, slot = blockIdx.z;
+  if (i >= d.W) return;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const unsigned long long mask = (unsigned long long)d.n - 1;
+  const long sigma = d.n / d.W, o = rp[3] + l;
+  double2 *a = (double2 *)d.man_tmp + (long)slot * 4 * d.W + (long)l * d.W;
+  a[i] = ld_x(d.inputs[slot], d.in_type, (long)((unsigned long long)(o + i * sigma) & mask));
+}
+
+__global__ void k_v3_man_interleave(V3Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, l = blockIdx.y, slot = blockIdx.z;
+  if (i >= d.W) return;
+  const double2 *a = (const double2 *)d.man_tmp + (long)slot * 4 * d.W + (long)l * d.W;
+  ((double2 *)d.man + (long)slot * 2 * d.W)[2 * i + l] = a[i];
+}
+
+int v3_max_smem_fft() { return 8192; }
 
 // ------------------------------------------------------------------ peel --
 
@@ -473,24 +495,35 @@ cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t s, StageEvents *se) 
   cudaError_t e;
   if ((e = cudaMemsetAsync(d.counters, 0, sizeof(int) * CNT_STRIDE * nslots, s))) return e;
   if ((e = cudaMemsetAsync(d.map_keys, 0xFF, sizeof(int) * (size_t)d.table_cap * nslots, s))) return e;
-  int Nmax = d.W;
-  if (d.B1 > Nmax) Nmax = d.B1;
-  if (d.B2 > Nmax) Nmax = d.B2;
+  int Nmax = d.B1 > d.B2 ? d.B1 : d.B2;
+  if (!d.large_man && d.W > Nmax) Nmax = d.W;
   int T = Nmax / 4;
   if (T > 1024) T = 1024;
   if (T < 32) T = 32;
   const int per = (Nmax / 4 + T - 1) / T;
   const size_t sm = (size_t)Nmax * sizeof(double2);
-  dim3 grid(6, nslots);
   mark(se, s);
+  int role0 = 0;
+  if (d.large_man) {
+    const dim3 g((d.W + 255) / 256, 2, nslots);
+    k_v3_man_gather<<<g, 256, 0, s>>>(d);
+    if ((e = cudaGetLastError())) return e;
+    double2 *a = (double2 *)d.man_tmp;
+    if ((e = global_fft_c128(a, a + 2L * d.W, d.W, 2, d.W, 4L * d.W, nslots, d.tw_man, s))) return e;
+    k_v3_man_interleave<<<g, 256, 0, s>>>(d);
+    if ((e = cudaGetLastError())) return e;
+    note_launches(2);
+    role0 = 2;
+  }
+  dim3 grid(6 - role0, nslots);
   switch (per) {
     case 1:
       if ((e = set_smem(k_v3_filters<1>, sm))) return e;
-      k_v3_filters<1><<<grid, T, sm, s>>>(d);
+      k_v3_filters<1><<<grid, T, sm, s>>>(d, role0);
       break;
     case 2:
       if ((e = set_smem(k_v3_filters<2>, sm))) return e;
-      k_v3_filters<2><<<grid, T, sm, s>>>(d);
+      k_v3_filters<2><<<grid, T, sm, s>>>(d, role0);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -73,3 +73,23 @@ def test_plans_identical_to_oracle(lib, oracle_lib, n, k, v):
         t, f = S.describe_filter(n, k, v, which)
         np.testing.assert_array_equal(t, op.filter_time(which))
         np.testing.assert_array_equal(f, op.filter_freq(which))
+
+
+def test_tuned_constants_lookup(lib):
+    """k buckets, and table-or-rule constants that always leave at least
+    2k+1 buckets (the algorithm's domain) for v1/v2 shapes."""
+    from sfft_gb300 import _lib
+    assert [lib.sfft_tuned_k(k) for k in (1, 16, 17, 100, 500, 512, 513)] == [16, 16, 32, 128, 512, 512, 1024]
+    import ctypes
+    import math
+    for n in (1 << 16, 1 << 19, 1 << 22):
+        for k in (10, 100, 500):
+            for v in (0, 1):
+                p = _lib.Params()
+                src = lib.sfft_tuned_params(n, k, v, ctypes.byref(p))
+                assert src in (0, 1)
+                s = math.sqrt(n * k / math.log2(n))
+                B = 1 << int(math.floor(math.log2(p.Bcst_loc * s)))
+                assert B >= 2 * k + 1
+                assert 1 <= p.threshold_loops <= p.loc_loops and p.est_loops >= 1
+    assert lib.sfft_tuned_params(1 << 16, 10, 2, ctypes.byref(_lib.Params())) == -1   # v3: none
