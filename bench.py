@@ -45,12 +45,18 @@ def args_():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--pool", type=int, default=64)
-    ap.add_argument("--only", default="all", choices=["all", "device", "uneven"],
+    ap.add_argument("--only", default="all", choices=["all", "device", "uneven", "stream"],
                     help="device: only the device-resident timed legs (for profiler captures); "
-                         "uneven: only the 256-signal uneven batch")
+                         "uneven: only the 256-signal uneven batch; stream: only the mixed serving stream")
+    ap.add_argument("--stream-requests", type=int, default=10000, help="requests in the mixed serving stream")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
+
+
+# Process-group backend: nccl on GPUs; gloo (SFFT_BENCH_BACKEND=gloo) lets
+# the rank logic run on CPU.
+BACKEND = os.environ.get("SFFT_BENCH_BACKEND", "nccl")
 
 
 def dist_init():
@@ -60,8 +66,11 @@ def dist_init():
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        if BACKEND == "nccl":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group(BACKEND)
     return ws, rank, local
 
 
@@ -72,11 +81,12 @@ def barrier(ws):
 
 
 def max_over_ranks(ws, v):
+    """The largest of the ranks' values (the job's time is its slowest rank's)."""
     if ws == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if BACKEND == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -265,6 +275,12 @@ def gb300_arm(a, ws, rank, local):
             stages = (list(ms)[:4], cnt)
         return total, per, launches, stages
 
+    if a.only == "stream":
+        if rank == 0:
+            print(json.dumps({"serving_stream_fp32": stream_leg(L, _lib, local, 1, a.stream_requests),
+                              "serving_stream_fp64": stream_leg(L, _lib, local, 0, a.stream_requests)}),
+                  flush=True)
+        return
     if a.only == "uneven":
         if rank == 0:
             print(json.dumps({"uneven_batch": uneven_leg(L, _lib, local),
@@ -277,6 +293,12 @@ def gb300_arm(a, ws, rank, local):
     clocks = clk.summary()
     t32max = max_over_ranks(ws, t32)
     value = ws * B * a.steps / (t32max / 1e3)
+    # ---- FP32 in the opt-in v2 voted mode (estimates voted candidates only)
+    p32v = sfft(N_SIG, K_SIG, VERSION, precision="fp32", device=local, max_batch=B)
+    if L.sfft_plan_v2_voted(p32v.sfft_plan, 1) != 0 or L.sfft_output_capacity(p32v.sfft_plan) > cap:
+        raise RuntimeError("voted mode: " + _lib.last_error())
+    t32v, per32v, _, st32v = timed(p32v, oval32, a.steps, a.warmup, profile=True)
+    value_voted = ws * B * a.steps / (max_over_ranks(ws, t32v) / 1e3)
     # ---- FP64 parity form
     s64 = max(3, a.steps // 8)
     t64, per64, _, st64 = timed(p64, oval64, s64, 3, profile=True)
@@ -285,7 +307,9 @@ def gb300_arm(a, ws, rank, local):
     if a.only == "device":
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "solves/s", "fp64_value": value64,
+                              "fp32_voted_value": value_voted,
                               "only": "device", "stage_ms_per_launch_fp32": stage_table(st32),
+                              "stage_ms_per_launch_fp32_voted": stage_table(st32v),
                               "stage_ms_per_launch_fp64": stage_table(st64)}), flush=True)
         return
 
@@ -310,7 +334,7 @@ def gb300_arm(a, ws, rank, local):
     serve64 = serving_leg(L, _lib, pool, 0, 0.8 * value64 / ws, 1500, local)
 
     # ---- accuracy: FP32 vs FP64 on the same draws, and both vs the truth
-    acc = accuracy(p32, p64, signals)
+    acc = accuracy(p32, p64, signals, p32v)
 
     # ---- roofline of the dominant stage (live CUDA events)
     roof, pipeline = roofline(p32, st32, B)
@@ -335,6 +359,12 @@ def gb300_arm(a, ws, rank, local):
                  "p50_ms": serve64["p50_ms"], "p99_ms": serve64["p99_ms"],
                  "batch_step_p50_ms": pct(per64, 50), "batch_step_p99_ms": pct(per64, 99),
                  "fp32_speedup": value / value64},
+        "fp32_voted": {"value": value_voted, "unit": "solves/s", "ms_per_step": max_over_ranks(ws, t32v) / a.steps,
+                       "batch_step_p50_ms": pct(per32v, 50), "batch_step_p99_ms": pct(per32v, 99),
+                       "stage_ms_per_launch": stage_table(st32v),
+                       "mode": "opt-in v2 voted mode (sfft_plan_v2_voted): only candidates that reach the vote "
+                               "threshold are estimated; the reference estimates and returns every comb "
+                               "candidate"},
         "latency_single_ms": {"fp32_p50": pct(lat32, 50), "fp32_p99": pct(lat32, 99),
                               "fp64_p50": pct(lat64, 50), "fp64_p99": pct(lat64, 99)},
         "accuracy": acc,
@@ -441,6 +471,128 @@ def uneven_leg(L, _lib, local, steps=20, warmup=3, precision=1):
                                   "mean_l1_on_support": float(np.mean(l1))},
             "workload": "256 v2 signals, n log-uniform 2^16..2^22, k uniform [10,500], |X|=1, 40 dB SNR, "
                         "seeds 0..255; autotuned constants per (n, k bucket); one CUDA graph per call"}
+
+
+def stream_requests(nreq, seed=42):
+    """The mixed serving stream: n log-uniform over 2^14..2^26, k uniform in
+    [1, min(2000, n/1024)], v2 (noisy, 30 dB SNR) or v3 (noiseless) 50/50,
+    complex64 or complex128 input 50/50, all drawn from one seeded stream."""
+    r = np.random.default_rng(seed)
+    out = []
+    for _ in range(nreq):
+        n = 1 << int(r.integers(14, 27))
+        k = int(r.integers(1, min(2000, n // 1024) + 1))
+        version = 3 if r.random() < 0.5 else 2
+        c64 = bool(r.random() < 0.5)
+        out.append((n, k, version, c64))
+    return out
+
+
+def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=0.8, seed=42):
+    """The mixed stream through the continuous-batching server: plans are
+    built once per (n, k bucket, version) and kept on the device under an
+    HBM budget; a closed-loop burst measures capacity, then the requests
+    arrive as a Poisson process at `load` x capacity."""
+    import threading
+    import torch
+    from sfft_gb300 import signals
+    reqs = stream_requests(nreq, seed)
+    dev = torch.device("cuda", local)
+    sig = {}
+
+    def signal_for(n, k, version, c64):
+        t = 1 << (k.bit_length() - 1)              # tones: largest power of two <= k
+        key = (n, t, version, c64)
+        if key not in sig:
+            base = (n, t, version, False)
+            if base not in sig:
+                x, _, _ = signals.make_signal_torch(n, t, (n * 31 + t) * 2 + version, device=dev,
+                                                    snr_db=30.0 if version == 2 else None)
+                sig[base] = x
+            if c64:
+                sig[key] = sig[base].to(torch.complex64)
+        return sig[key]
+
+    ptr = [ctypes.c_void_p(signal_for(*q).data_ptr()) for q in reqs]
+    torch.cuda.synchronize()
+    sig_bytes = sum(x.numel() * x.element_size() for x in sig.values())
+    opts = _lib.ServerOptions(local, max_batch, int(budget_gb * (1 << 30)), 2, 2)
+    srv = L.sfft_server_create(ctypes.byref(opts))
+    if not srv:
+        return {"error": _lib.last_error()}
+    lat = ctypes.c_double()
+
+    def submit(i, seed_):
+        n, k, version, c64 = reqs[i]
+        return L.sfft_server_submit(srv, n, k, version - 1, precision, ptr[i], 1 if c64 else 0, seed_)
+
+    def wait(rid):
+        c = L.sfft_server_wait(srv, rid, None, None, 0, ctypes.byref(lat))
+        return c, lat.value
+
+    # plans: one request per distinct plan, outside the timed region
+    t0 = time.perf_counter()
+    first = {}
+    for i, (n, k, version, c64) in enumerate(reqs):
+        kk = L.sfft_tuned_k(k) if version == 2 else max(8, 1 << (max(k, 1) - 1).bit_length())
+        first.setdefault((n, kk, version), i)
+    fails = 0
+    for i in first.values():
+        c, _ = wait(submit(i, i))
+        fails += c < 0
+    plan_s = time.perf_counter() - t0
+    # capacity: every request submitted at once
+    burst = min(nreq, 2000)
+    t0 = time.perf_counter()
+    ids = [submit(i, 7 + i) for i in range(burst)]
+    for rid in ids:
+        wait(rid)
+    capacity = burst / (time.perf_counter() - t0)
+    # the timed stream
+    rate = load * capacity
+    gaps = np.random.default_rng(seed + 1).exponential(1.0 / rate, size=nreq)
+    ids = [None] * nreq
+    lats = [0.0] * nreq
+    failed = [0]
+    done_t = [0.0]
+
+    def waiter():
+        for i in range(nreq):
+            while ids[i] is None:
+                time.sleep(0)
+            c, ms = wait(ids[i])
+            lats[i] = ms
+            failed[0] += c < 0
+        done_t[0] = time.perf_counter()
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    t_next = t0
+    for i in range(nreq):
+        t_next += gaps[i]
+        while time.perf_counter() < t_next:
+            pass
+        ids[i] = submit(i, 100000 + i)
+    th.join()
+    stats = (ctypes.c_long * 8)()
+    L.sfft_server_stats(srv, stats, 8)
+    L.sfft_server_destroy(srv)
+    by_v = {v: [lats[i] for i in range(nreq) if reqs[i][2] == v] for v in (2, 3)}
+    del sig
+    torch.cuda.empty_cache()
+    return {"requests": nreq, "precision": "fp32" if precision == 1 else "fp64 (v3 always fp64)",
+            "solves_per_s": nreq / (done_t[0] - t0), "offered_rate": rate, "capacity_burst_solves_per_s": capacity,
+            "p50_ms": pct(lats, 50), "p99_ms": pct(lats, 99),
+            "p50_ms_v2": pct(by_v[2], 50), "p99_ms_v2": pct(by_v[2], 99),
+            "p50_ms_v3": pct(by_v[3], 50), "p99_ms_v3": pct(by_v[3], 99),
+            "failed": failed[0] + fails, "plans_built": len(first), "plan_build_s": plan_s,
+            "batches": int(stats[0]), "plans_evicted": int(stats[2]), "deferred": int(stats[3]),
+            "hbm_budget_gb": budget_gb, "signal_pool_gb": sig_bytes / 2**30,
+            "workload": "n log-uniform 2^14..2^26, k uniform [1, min(2000, n/1024)], v2 (30 dB SNR) or v3 "
+                        "(noiseless) 50/50, complex64/complex128 50/50, seed 42; Poisson arrivals at "
+                        f"{load:.0%} of the burst capacity; v1/v2 autotuned per (n, k bucket), v3 k rounded "
+                        "up to a power of two (at least 8)"}
 
 
 def serving_leg(L, _lib, pool, precision, rate, nreq, device):
@@ -570,7 +722,7 @@ def roofline(p32, st32, B):
     return roof, pipeline
 
 
-def accuracy(p32, p64, signals):
+def accuracy(p32, p64, signals, p32v=None):
     from oracle import oracle as O
     x, pos, vals = signals.make_signal(N_SIG, K_SIG, SEED, mag=MAG, snr_db=SNR)
     O.seed_libc(SEED)
@@ -595,6 +747,19 @@ def accuracy(p32, p64, signals):
         spurious = int(np.sum(found)) - (len(pos) - missed)
         res[f"{name}_vs_truth"] = {"mean_l1_on_support": float(np.mean(np.abs(est[pos] - vals))),
                                    "missed": missed, "spurious": spurious, "tau": tau}
+    if p32v is not None:
+        # voted mode: the recovered support (|X| >= tau) and its values against FP64
+        O.seed_libc(SEED)
+        iv, vv = p32v.execute_sparse(x)
+        ev, e64 = np.zeros(N_SIG, dtype=complex), np.zeros(N_SIG, dtype=complex)
+        ev[iv] = np.conj(vv)
+        e64[i64] = np.conj(v64)
+        tau = 0.5 * float(np.min(np.abs(vals)))
+        sv, s64 = np.nonzero(np.abs(ev) >= tau)[0], np.nonzero(np.abs(e64) >= tau)[0]
+        d = ev[s64] - e64[s64]
+        res["fp32_voted_vs_fp64"] = {"recovered_support_identical": bool(np.array_equal(sv, s64)),
+                                     "max_l1_on_recovered_support": float(np.max(np.abs(d.real) + np.abs(d.imag))),
+                                     "outputs": int(iv.size), "fp64_outputs": int(i64.size), "tau": tau}
     return res
 
 

@@ -261,6 +261,15 @@ int sfft_mixed_groups(const sfft_mixed *m);
 void *sfft_mixed_stream(const sfft_mixed *m);
 void sfft_mixed_destroy(sfft_mixed *m);
 
+/* ---- v2 voted mode (no counterpart in the reference) ------------------ */
+
+/* on = 1: the v2 plan estimates only the candidates that reached the vote
+ * threshold (as v1 does) instead of every comb candidate, which the
+ * reference estimates and returns (most of them noise).  The recovered
+ * tones are the same; the result is not the reference's output list.
+ * Call between executions; the output capacity may change.  0 or -1. */
+int sfft_plan_v2_voted(sfft_plan *plan, int on);
+
 /* ---- constants chosen by this project (no counterpart in the reference) */
 
 /* v1/v2 constants for (n, k): the autotuner's table row for n and the k

@@ -114,6 +114,7 @@ std::vector<float> to_f32(const std::vector<double> &v) {
 
 struct PlanImpl {
   int version = 0, n = 0, k = 0, prec = sfft::PREC_FP64, device = 0, max_batch = 16;
+  int voted = 0;  // v2: estimate voted candidates only (opt-in, not the reference's output)
   sfft::V12Params p12;
   sfft::V3Params p3;
   cudaStream_t stream = nullptr;
@@ -297,11 +298,12 @@ bool ensure_slots(PlanImpl &P, int want) {
     const int L = L12(P);
     P.rp_stride = 2 * L + p.Comb_loops + 1;
     const int q = P.n / p.B_loc;
-    P.hit_cap = P.version == 0
+    P.hit_cap = P.version == 0 || P.voted
                     ? (int)std::min<long>((long)P.n, ((long)p.loops_loc * p.B_thresh * q) / p.loops_thresh + 1)
                     : 1;
     const long comb_max = std::min<long>((long)p.W_Comb, (long)p.Comb_loops * p.B_thresh);
     P.out_cap = P.version == 0 ? P.hit_cap : (int)(comb_max * (P.n / p.W_Comb));
+    if (P.voted) P.out_cap = std::max(P.out_cap, P.hit_cap);
     if (P.prec == sfft::PREC_FP64 && !P.xs32.ensure(8 * p.x_samp_size * S)) return false;
     if (P.large_b && !P.xs_tmp.ensure(cs * p.x_samp_size * S)) return false;
     if (P.large_c && (!P.comb_buf.ensure(cs * (size_t)p.Comb_loops * p.W_Comb * S) ||
@@ -463,6 +465,7 @@ sfft::V12Dev v12_view(PlanImpl &P) {
   d.out_count = nullptr;
   d.hit_cap = P.hit_cap;
   d.out_cap = P.out_cap;
+  d.voted = P.voted;
   d.out_stride = P.out_cap;
   d.rparams = P.rparams.as<int>();
   d.rp_stride = P.rp_stride;
@@ -1117,6 +1120,21 @@ long sfft_plan_footprint(const sfft_plan *plan) {
   long total = 0;
   for (const DBuf *b : bufs) total += (long)b->bytes;
   return total;
+}
+
+int sfft_plan_v2_voted(sfft_plan *plan, int on) {
+  PlanImpl *P = plan ? (PlanImpl *)plan->data : nullptr;
+  if (!P || P->version != 1) {
+    set_err("the voted mode applies to v2 plans");
+    return -1;
+  }
+  std::lock_guard<std::mutex> g(P->mu);
+  if (!cuda_ok(cudaSetDevice(P->device), "cudaSetDevice") || !cuda_ok(cudaStreamSynchronize(P->stream), "sync"))
+    return -1;
+  P->voted = on ? 1 : 0;
+  const int slots = P->slots;
+  P->slots = 0;  // re-derive capacities and grow the buffers they need
+  return ensure_slots(*P, std::max(1, slots)) ? 0 : -1;
 }
 
 long sfft_output_capacity(const sfft_plan *plan) {

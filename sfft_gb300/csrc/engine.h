@@ -59,6 +59,7 @@ struct V12Dev {
   void *out_val;            // out_stride complex per slot (R2)
   int *out_count;           // optional: per-slot coefficient count
   int hit_cap, out_cap;
+  int voted;                // v2: estimate only candidates that reached the vote threshold
   long out_stride;
   // per-exec inputs
   const int *rparams;       // per slot: a[L], ai[L], comb_offsets[comb_loops], epoch

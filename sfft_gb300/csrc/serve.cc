@@ -151,12 +151,14 @@ long device_free() {
   return (long)f;
 }
 
-// Evicts idle plans (least recently used first) until `need` more bytes fit.
-bool make_room(sfft_server *s, long need) {
+// Evicts idle plans (least recently used first, never `keep`) until `need`
+// more bytes fit.
+bool make_room(sfft_server *s, long need, const PlanEntry *keep = nullptr) {
   while (s->held + need > s->budget) {
     PlanEntry *victim = nullptr;
     for (auto &kv : s->plans)
-      if (!kv.second->busy.load() && (!victim || kv.second->last_used < victim->last_used)) victim = kv.second;
+      if (kv.second != keep && !kv.second->busy.load() && (!victim || kv.second->last_used < victim->last_used))
+        victim = kv.second;
     if (!victim) return false;
     s->held -= victim->bytes;
     sfft_free_plan(victim->plan);
@@ -193,7 +195,10 @@ long estimate_bytes(const PlanKey &key, int slots, int tune) {
 
 PlanEntry *get_plan(sfft_server *s, const PlanKey &key, std::string &err) {
   auto it = s->plans.find(key);
-  if (it != s->plans.end()) return it->second;
+  if (it != s->plans.end()) {
+    it->second->last_used = ++s->tick;  // most recently used
+    return it->second;
+  }
   const long need = estimate_bytes(key, s->max_batch, s->tune_invalid);
   if (need > s->budget) {
     err = "request needs more device memory than the server's budget";
@@ -263,7 +268,12 @@ void schedule(sfft_server *s) {
     long sbytes = 0;
     for (Request *r : b->reqs)
       if (!r->staged && r->in_type >= 100) sbytes += (long)r->n * ((r->in_type - 100) == SFFT_IN_C64 ? 8 : 16);
-    if (!make_room(s, obytes + sbytes)) {
+    if (pe->bytes + obytes + sbytes > s->budget) {  // would never fit
+      for (Request *r : b->reqs) fail(s, r, "batch and plan need more device memory than the server's budget");
+      delete b;
+      continue;
+    }
+    if (!make_room(s, obytes + sbytes, pe)) {  // the batch's own plan stays
       for (Request *r : b->reqs) keep.push_back(r);
       delete b;
       s->n_deferred++;

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256) k_vote(V12Dev d) {
     }
     if ((int)(nv & 255u) == d.thresh) {
       atomicAdd(&cnt[CNT_VOTED], 1);
-      if (d.version == 0) {
+      if (d.version == 0 || d.voted) {
         const int pos = atomicAdd(&cnt[CNT_HITS], 1);
         if (pos < d.hit_cap)
           d.hits[(long)slot * d.hit_cap + pos] = (int)f;
@@ -565,10 +565,11 @@ __device__ __noinline__ double2 median64_exact(const V12Dev &d, const double2 *x
   return make_double2(mre, mim);
 }
 
-// Number of candidates of a slot: v1 hits, v2 every comb candidate.
+// Number of candidates of a slot: v1 hits, v2 every comb candidate (or,
+// in the opt-in voted mode, v2 hits).
 __device__ __forceinline__ long cand_total(const V12Dev &d, int slot) {
   const int *cnt = d.counters + slot * CNT_STRIDE;
-  if (d.version == 0) return min(cnt[CNT_HITS], d.hit_cap);
+  if (d.version == 0 || d.voted) return min(cnt[CNT_HITS], d.hit_cap);
   return (long)cnt[CNT_COMB] * (d.n / d.W);
 }
 
@@ -578,7 +579,7 @@ __device__ __forceinline__ long cand_total(const V12Dev &d, int slot) {
 // (which depends on the residue only when the window length n / B divides
 // W) is one broadcast load.  The output is a set; its order is free.
 __device__ __forceinline__ unsigned cand_freq(const V12Dev &d, int slot, long h) {
-  if (d.version == 0) return (unsigned)d.hits[(long)slot * d.hit_cap + h];
+  if (d.version == 0 || d.voted) return (unsigned)d.hits[(long)slot * d.hit_cap + h];
   const unsigned reps = (unsigned)(d.n / d.W);  // a power of two
   const unsigned hu = (unsigned)h, ridx = hu >> (__ffs(reps) - 1), rep = hu & (reps - 1);
   return rep * (unsigned)d.W + (unsigned)d.comb_list[(long)slot * d.W + ridx];

@@ -123,3 +123,33 @@ def test_tuned_constants_outside_reference_domain(env):
     est = np.zeros(n, dtype=complex)
     est[gi] = np.conj(gv)
     assert np.max(np.abs(est[pos] - vals)) < 0.05   # every tone recovered (the autotuner's bar)
+
+
+def test_batch_never_evicts_its_own_plan(env):
+    """Two cached plans and a budget with room for both but not for a batch
+    as well: a batch for the least recently used plan must evict the other
+    plan, never its own (which it is about to run on)."""
+    torch, _lib, L, O = env
+    from sfft_gb300 import signals
+    shapes = [(1 << 16, 50, 2), (1 << 17, 50, 2)]
+    xs = [torch.from_numpy(signals.make_signal(n, k, 21)[0]).cuda() for n, k, _ in shapes]
+    need = [L.sfft_server_plan_bytes(n, k, v - 1, 0, 2) for n, k, v in shapes]
+    alone = []
+    for (n, k, v), x in zip(shapes, xs):
+        s = _server(L, _lib, max_batch=2)
+        alone.append(_wait(L, _lib, s, L.sfft_server_submit(s, n, k, v - 1, 0, ctypes.c_void_p(x.data_ptr()), 0, 5),
+                           1 << 20))
+        L.sfft_server_destroy(s)
+    s = _server(L, _lib, max_batch=2, budget=int(1.05 * (need[0] + need[1])))
+    got = []
+    for rep in range(3):
+        for j, ((n, k, v), x) in enumerate(zip(shapes, xs)):
+            rid = L.sfft_server_submit(s, n, k, v - 1, 0, ctypes.c_void_p(x.data_ptr()), 0, 5)
+            got.append((j, _wait(L, _lib, s, rid, 1 << 20)))
+    stats = (ctypes.c_long * 8)()
+    L.sfft_server_stats(s, stats, 8)
+    L.sfft_server_destroy(s)
+    for j, (gi, gv, _) in got:
+        np.testing.assert_array_equal(gi, alone[j][0])
+        np.testing.assert_array_equal(gv, alone[j][1])
+    assert stats[5] <= stats[6]
