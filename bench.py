@@ -516,7 +516,8 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
     ptr = [ctypes.c_void_p(signal_for(*q).data_ptr()) for q in reqs]
     torch.cuda.synchronize()
     sig_bytes = sum(x.numel() * x.element_size() for x in sig.values())
-    opts = _lib.ServerOptions(local, max_batch, int(budget_gb * (1 << 30)), 2, 2)
+    voted = 1 if precision == 1 else 0          # the FP32 serving form runs v2 in the voted mode
+    opts = _lib.ServerOptions(local, max_batch, int(budget_gb * (1 << 30)), 2, 2, voted)
     srv = L.sfft_server_create(ctypes.byref(opts))
     if not srv:
         return {"error": _lib.last_error()}
@@ -575,8 +576,8 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
             pass
         ids[i] = submit(i, 100000 + i)
     th.join()
-    stats = (ctypes.c_long * 8)()
-    L.sfft_server_stats(srv, stats, 8)
+    stats = (ctypes.c_long * 9)()
+    L.sfft_server_stats(srv, stats, 9)
     L.sfft_server_destroy(srv)
     by_v = {v: [lats[i] for i in range(nreq) if reqs[i][2] == v] for v in (2, 3)}
     del sig
@@ -588,6 +589,7 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
             "p50_ms_v3": pct(by_v[3], 50), "p99_ms_v3": pct(by_v[3], 99),
             "failed": failed[0] + fails, "plans_built": len(first), "plan_build_s": plan_s,
             "batches": int(stats[0]), "plans_evicted": int(stats[2]), "deferred": int(stats[3]),
+            "batches_spilled_to_host": int(stats[8]), "v2_mode": "voted" if voted else "reference (all comb candidates)",
             "hbm_budget_gb": budget_gb, "signal_pool_gb": sig_bytes / 2**30,
             "workload": "n log-uniform 2^14..2^26, k uniform [1, min(2000, n/1024)], v2 (30 dB SNR) or v3 "
                         "(noiseless) 50/50, complex64/complex128 50/50, seed 42; Poisson arrivals at "

@@ -214,6 +214,7 @@ struct sfft_server_options
   int tune_invalid;             /* v1/v2: 1 shapes outside the reference's domain get tuned constants;
                                    2 every v1/v2 request uses autotuned constants, k rounded to its bucket;
                                    1 and 2: v3 requests with k < 8 run on the smallest v3 plan (k = 8) */
+  int v2_voted;                 /* 1: v2 plans in the voted mode (sfft_plan_v2_voted) */
 };
 typedef struct sfft_server_options sfft_server_options;
 
@@ -231,7 +232,8 @@ long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val,
  * `max_batch` slots (its admission estimate), or -1. */
 long sfft_server_plan_bytes(int n, int k, enum sfft_version version, int precision, int max_batch);
 /* batches, plans made, plans evicted, deferrals, cached plans, bytes held,
- * budget, queued requests. */
+ * budget, queued requests, batches whose results were moved to host memory
+ * (finished, not yet collected, and their device memory needed). */
 int sfft_server_stats(sfft_server *s, long *stats, int nstats);
 
 /* ---- signals of different shapes in one CUDA graph ---------------------- */

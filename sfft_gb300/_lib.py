@@ -31,7 +31,7 @@ class Params(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("max_batch", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_long),
-                ("k_round", ctypes.c_int), ("tune_invalid", ctypes.c_int)]
+                ("k_round", ctypes.c_int), ("tune_invalid", ctypes.c_int), ("v2_voted", ctypes.c_int)]
 
 
 class Plan(ctypes.Structure):

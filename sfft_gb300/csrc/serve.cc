@@ -83,29 +83,37 @@ struct Batch {
   Server *srv = nullptr;
   PlanEntry *pe = nullptr;
   std::vector<Request *> reqs;
+  std::vector<char> taken;  // per slot: its request was collected (and deleted)
   int *d_idx = nullptr;
   void *d_val = nullptr;
   int *d_cnt = nullptr;
   long bytes = 0, cap = 0;
   int collected = 0;
   size_t val_size = 16;
+  std::atomic<bool> complete{false};
+  // results moved to host memory to free the device (see spill_batch)
+  bool spilled = false;
+  std::vector<int> h_cnt;
+  std::vector<std::vector<int>> h_idx;
+  std::vector<std::vector<char>> h_val;
 };
 
 }  // namespace
 
 struct sfft_server {
-  int device = 0, max_batch = 32, k_round = 0, tune_invalid = 0;
+  int device = 0, max_batch = 32, k_round = 0, tune_invalid = 0, v2_voted = 0;
   long budget = 0, held = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request *> queue;
   std::unordered_map<long, Request *> reqs;
   std::map<PlanKey, PlanEntry *> plans;
+  std::list<Batch *> batches;  // launched and not yet fully collected, oldest first
   long next_id = 1, tick = 0;
   bool stop = false;
   std::thread worker;
   // statistics
-  long n_batches = 0, n_evicted = 0, n_plans = 0, n_deferred = 0;
+  long n_batches = 0, n_evicted = 0, n_plans = 0, n_deferred = 0, n_spilled = 0;
 };
 
 namespace {
@@ -123,6 +131,7 @@ void host_done(void *arg) {
     r->t_done = now;
     r->done.store(true, std::memory_order_release);
   }
+  b->complete.store(true, std::memory_order_release);
   b->pe->busy.store(false, std::memory_order_release);
   s->cv_done.notify_all();
   s->cv_work.notify_all();
@@ -151,15 +160,75 @@ long device_free() {
   return (long)f;
 }
 
-// Evicts idle plans (least recently used first, never `keep`) until `need`
-// more bytes fit.
+void free_batch_device(Batch *b) {
+  cudaFree(b->d_idx);
+  cudaFree(b->d_val);
+  cudaFree(b->d_cnt);
+  b->d_idx = nullptr;
+  b->d_val = nullptr;
+  b->d_cnt = nullptr;
+  for (size_t i = 0; i < b->reqs.size(); i++)
+    if (!b->taken[i] && b->reqs[i]->staged) {
+      cudaFree(b->reqs[i]->staged);
+      b->reqs[i]->staged = nullptr;
+    }
+}
+
+// Moves a finished batch's uncollected results to host memory and frees its
+// device memory.  Results are held until their requests are waited for, in
+// any order; without spilling, a client that waits for an early request
+// while later requests' results fill the budget would never see the early
+// one admitted.
+bool spill_batch(sfft_server *s, Batch *b) {
+  cudaSetDevice(s->device);
+  const int m = (int)b->reqs.size();
+  b->h_cnt.assign(m, 0);
+  b->h_idx.resize(m);
+  b->h_val.resize(m);
+  if (cudaMemcpy(b->h_cnt.data(), b->d_cnt, sizeof(int) * m, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  for (int i = 0; i < m; i++) {
+    if (b->taken[i]) continue;
+    const long c = std::max(0L, std::min((long)b->h_cnt[i], b->cap));
+    b->h_idx[i].resize(c);
+    b->h_val[i].resize(c * b->val_size);
+    if (c && (cudaMemcpy(b->h_idx[i].data(), b->d_idx + (size_t)i * b->cap, sizeof(int) * c,
+                         cudaMemcpyDeviceToHost) != cudaSuccess ||
+              cudaMemcpy(b->h_val[i].data(), (char *)b->d_val + b->val_size * (size_t)i * b->cap,
+                         b->val_size * c, cudaMemcpyDeviceToHost) != cudaSuccess)) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  free_batch_device(b);
+  b->spilled = true;
+  s->held -= b->bytes;
+  b->bytes = 0;
+  s->n_spilled++;
+  return true;
+}
+
+// Makes `need` more bytes fit the budget: evicts idle plans (least recently
+// used first, never `keep`), then spills finished batches' results to host
+// memory (oldest first).
 bool make_room(sfft_server *s, long need, const PlanEntry *keep = nullptr) {
   while (s->held + need > s->budget) {
     PlanEntry *victim = nullptr;
     for (auto &kv : s->plans)
       if (kv.second != keep && !kv.second->busy.load() && (!victim || kv.second->last_used < victim->last_used))
         victim = kv.second;
-    if (!victim) return false;
+    if (!victim) {
+      Batch *sp = nullptr;
+      for (Batch *b : s->batches)
+        if (!b->spilled && b->complete.load(std::memory_order_acquire)) {
+          sp = b;
+          break;
+        }
+      if (!sp || !spill_batch(s, sp)) return false;
+      continue;
+    }
     s->held -= victim->bytes;
     sfft_free_plan(victim->plan);
     s->plans.erase(victim->key);
@@ -208,6 +277,10 @@ PlanEntry *get_plan(sfft_server *s, const PlanKey &key, std::string &err) {
   sfft_options o{key.prec, s->device, s->max_batch};
   bool tuned = false;
   sfft_plan *p = sfft::make_plan_tuned(key.n, key.k, key.version, o, s->tune_invalid, tuned);
+  if (p && s->v2_voted && key.version == SFFT_VERSION_2 && sfft_plan_v2_voted(p, 1) != 0) {
+    sfft_free_plan(p);
+    p = nullptr;
+  }
   if (!p) {
     err = sfft_last_error();
     return nullptr;
@@ -263,6 +336,7 @@ void schedule(sfft_server *s) {
     b->val_size = (key.version < 2 && key.prec == SFFT_PREC_FP32) ? 8 : 16;
     b->cap = pe->cap;
     b->reqs.assign(g.second.begin(), g.second.begin() + m);
+    b->taken.assign(m, 0);
     for (int i = m; i < (int)g.second.size(); i++) keep.push_back(g.second[i]);
     const long obytes = (long)m * pe->cap * (4 + (long)b->val_size) + 4L * m;
     long sbytes = 0;
@@ -310,6 +384,7 @@ void schedule(sfft_server *s) {
       ok = sfft_exec_batch_ex(pe->plan, m, ins.data(), in_type, seeds.data(), b->d_idx, b->d_val, b->d_cnt,
                               pe->cap, st) == 0;
     if (ok) ok = cudaLaunchHostFunc(st, host_done, b) == cudaSuccess;
+    if (ok) s->batches.push_back(b);
     if (!ok) {
       cudaGetLastError();
       const std::string e = std::string("batch launch failed: ") + sfft_last_error();
@@ -351,6 +426,7 @@ sfft_server *sfft_server_create(const sfft_server_options *opt) {
     s->budget = opt->hbm_budget_bytes;
     s->k_round = opt->k_round;
     s->tune_invalid = opt->tune_invalid;
+    s->v2_voted = opt->v2_voted;
   }
   cudaSetDevice(s->device);
   if (s->budget <= 0) s->budget = (long)(0.8 * device_free());
@@ -368,6 +444,10 @@ void sfft_server_destroy(sfft_server *s) {
   s->worker.join();
   cudaSetDevice(s->device);
   cudaDeviceSynchronize();
+  for (Batch *b : s->batches) {  // uncollected results
+    if (!b->spilled) free_batch_device(b);
+    delete b;
+  }
   for (auto &kv : s->plans) {
     sfft_free_plan(kv.second->plan);
     delete kv.second;
@@ -424,35 +504,56 @@ long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val,
     Batch *b = r->batch;
     cudaSetDevice(s->device);
     int cnt = 0;
-    bool ok = cudaMemcpy(&cnt, b->d_cnt + r->slot, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+    bool ok = true;
+    if (b->spilled)
+      cnt = (int)b->h_idx[r->slot].size();
+    else
+      ok = cudaMemcpy(&cnt, b->d_cnt + r->slot, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
     if (ok && cnt > cap) {
       sfft::set_last_error("output capacity too small");
       ok = false;
     }
-    if (ok && out_idx)
-      ok = cudaMemcpy(out_idx, b->d_idx + (size_t)r->slot * b->cap, sizeof(int) * cnt, cudaMemcpyDefault) ==
-           cudaSuccess;
+    if (ok && out_idx) {
+      if (b->spilled)
+        std::memcpy(out_idx, b->h_idx[r->slot].data(), sizeof(int) * (size_t)cnt);
+      else
+        ok = cudaMemcpy(out_idx, b->d_idx + (size_t)r->slot * b->cap, sizeof(int) * cnt, cudaMemcpyDefault) ==
+             cudaSuccess;
+    }
     if (ok && out_val) {
-      if (b->val_size == 16) {
-        ok = cudaMemcpy(out_val, (char *)b->d_val + 16 * (size_t)r->slot * b->cap, 16 * (size_t)cnt,
-                        cudaMemcpyDefault) == cudaSuccess;
+      std::vector<char> tmp;
+      const char *src = nullptr;
+      if (b->spilled) {
+        src = b->h_val[r->slot].data();
       } else {
-        std::vector<float> tmp(2 * (size_t)cnt);
-        ok = cudaMemcpy(tmp.data(), (char *)b->d_val + 8 * (size_t)r->slot * b->cap, 8 * (size_t)cnt,
-                        cudaMemcpyDeviceToHost) == cudaSuccess;
+        tmp.resize(b->val_size * (size_t)cnt);
+        ok = cudaMemcpy(tmp.data(), (char *)b->d_val + b->val_size * (size_t)r->slot * b->cap,
+                        b->val_size * (size_t)cnt, cudaMemcpyDeviceToHost) == cudaSuccess;
+        src = tmp.data();
+      }
+      if (ok && b->val_size == 16) {
+        std::memcpy(out_val, src, 16 * (size_t)cnt);
+      } else if (ok) {
+        const float *f = (const float *)src;
         double *o = (double *)out_val;
-        for (size_t i = 0; ok && i < tmp.size(); i++) o[i] = tmp[i];
+        for (size_t i = 0; i < 2 * (size_t)cnt; i++) o[i] = f[i];
       }
     }
     if (ok) result = cnt;
+    if (r->staged) {  // the batch is complete: its staged input is no longer read
+      cudaFree(r->staged);
+      r->staged = nullptr;
+    }
+    b->taken[r->slot] = 1;  // r is deleted below: the batch must not touch it again
+    if (b->spilled) {
+      std::vector<int>().swap(b->h_idx[r->slot]);
+      std::vector<char>().swap(b->h_val[r->slot]);
+    }
     // the batch's memory goes once all its requests are collected
-    if (++b->collected == (int)b->reqs.size()) {  // the batch finished: free on any stream
-      cudaFreeAsync(b->d_idx, 0);
-      cudaFreeAsync(b->d_val, 0);
-      cudaFreeAsync(b->d_cnt, 0);
-      for (Request *q : b->reqs)
-        if (q->staged) cudaFreeAsync(q->staged, 0);
+    if (++b->collected == (int)b->reqs.size()) {
+      if (!b->spilled) free_batch_device(b);  // every slot is taken: no request is touched
       s->held -= b->bytes;
+      s->batches.remove(b);
       delete b;
     }
   }
@@ -473,7 +574,7 @@ int sfft_server_stats(sfft_server *s, long *stats, int nstats) {
   if (!s || !stats) return -1;
   std::lock_guard<std::mutex> g(s->mu);
   const long v[] = {s->n_batches, s->n_plans, s->n_evicted, s->n_deferred, (long)s->plans.size(), s->held,
-                    s->budget, (long)s->queue.size()};
+                    s->budget, (long)s->queue.size(), s->n_spilled};
   const int m = std::min(nstats, (int)(sizeof v / sizeof v[0]));
   for (int i = 0; i < m; i++) stats[i] = v[i];
   return m;

@@ -90,6 +90,69 @@ __global__ void __launch_bounds__(256) k_fold(V12Dev d) {
   ((c2_t<R> *)d.xs)[(long)slot * d.xs_size + g] = acc;
 }
 
+// FP32 form of the fold with each bucket's taps split over S adjacent
+// lanes (tap m of the bucket goes to lane m mod S), the S partial sums
+// combined by shuffles.  A signal then spans S times as many threads as
+// buckets, so the GPU's resident threads work on about one signal at a
+// time: that signal's input stays in L2 while all its loops gather from it,
+// instead of several signals' inputs contending for L2 and being fetched
+// from DRAM repeatedly.  The summation order differs from the reference's,
+// which the FP32 form does not reproduce anyway.
+template <typename In, int S>
+__global__ void __launch_bounds__(256) k_fold_split(V12Dev d) {
+  const int slot = blockIdx.y;
+  const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long g = gt / S;
+  const int part = (int)(gt % S);
+  const bool live = g < d.xs_size;
+  const long locsz = (long)d.L_loc * d.B_loc;
+  int j = 0, b = 0, B = 1, w = 0;
+  const float2 *taps = nullptr;
+  if (live) {
+    if (g < locsz) {
+      j = (int)(g / d.B_loc);
+      b = (int)(g & (d.B_loc - 1));
+      B = d.B_loc;
+      w = d.w_loc;
+      taps = (const float2 *)d.taps_loc;
+    } else {
+      const long h = g - locsz;
+      j = d.L_loc + (int)(h / d.B_est);
+      b = (int)(h & (d.B_est - 1));
+      B = d.B_est;
+      w = d.w_est;
+      taps = (const float2 *)d.taps_est;
+    }
+  }
+  float2 acc = make_float2(0.f, 0.f);
+  if (live) {
+    const int *rp = d.rparams + (long)slot * d.rp_stride;
+    const unsigned ai = (unsigned)rp[d.L + j], mask = (unsigned)d.n - 1u;
+    const In *x = (const In *)d.inputs[slot];
+    const int step = S * B;
+    for (int t0 = b + part * B; t0 < w; t0 += 4 * step) {
+      float2 xv[4], hv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int t = t0 + u * step;
+        if (t < w) {
+          xv[u] = cvt_in<float>(__ldg(x + (((unsigned)t * ai) & mask)));
+          hv[u] = __ldg(taps + t);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (t0 + u * step < w) acc = cadd<float>(acc, cmul<float>(xv[u], hv[u]));
+    }
+  }
+#pragma unroll
+  for (int o = S / 2; o > 0; o >>= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+  }
+  if (live && part == 0) ((float2 *)d.xs)[(long)slot * d.xs_size + g] = acc;
+}
+
 // ---------------------------------------------------------- smem layout --
 
 template <typename R>
@@ -885,6 +948,15 @@ static cudaError_t launch_estimate(const V12Dev &d, int nslots, cudaStream_t s) 
   return dispatch_estimate<k_estimate32_k>(d, nslots, sm_count(), s);
 }
 
+// The split FP32 fold is the default (SFFT_GB300_FOLD_SPLIT=0 turns it off).
+static bool fold_split() {
+  static const bool on = [] {
+    const char *e = getenv("SFFT_GB300_FOLD_SPLIT");
+    return !e || atoi(e) != 0;
+  }();
+  return on;
+}
+
 template <typename R, typename In>
 static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageEvents *se) {
   cudaError_t e;
@@ -911,8 +983,14 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
     note_launches(1);
   }
   mark(se, s);
-  dim3 fg((unsigned)((d.xs_size + 255) / 256), nslots);
-  k_fold<R, In><<<fg, 256, 0, s>>>(d);
+  if (sizeof(R) == 4 && fold_split()) {
+    constexpr int S = 4;
+    dim3 fg((unsigned)((d.xs_size * S + 255) / 256), nslots);
+    k_fold_split<In, S><<<fg, 256, 0, s>>>(d);
+  } else {
+    dim3 fg((unsigned)((d.xs_size + 255) / 256), nslots);
+    k_fold<R, In><<<fg, 256, 0, s>>>(d);
+  }
   if ((e = cudaGetLastError())) return e;
   mark(se, s);
   if (!d.large_buckets) {

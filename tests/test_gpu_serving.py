@@ -153,3 +153,34 @@ def test_batch_never_evicts_its_own_plan(env):
         np.testing.assert_array_equal(gi, alone[j][0])
         np.testing.assert_array_equal(gv, alone[j][1])
     assert stats[5] <= stats[6]
+
+
+def test_in_order_waits_complete_when_results_fill_the_budget(env):
+    """Many requests submitted at once under a budget that holds the plans
+    but not all the batches' results, then waited for in submission order:
+    finished, uncollected results move to host memory so that earlier
+    requests are still admitted, and every result equals the request run
+    alone."""
+    torch, _lib, L, O = env
+    from sfft_gb300 import signals
+    shapes = [(1 << 16, 50, 2), (1 << 17, 50, 2)]
+    xs = [torch.from_numpy(signals.make_signal(n, k, 31)[0]).cuda() for n, k, _ in shapes]
+    need = [L.sfft_server_plan_bytes(n, k, v - 1, 0, 2) for n, k, v in shapes]
+    alone = []
+    for (n, k, v), x in zip(shapes, xs):
+        s = _server(L, _lib, max_batch=2)
+        alone.append(_wait(L, _lib, s, L.sfft_server_submit(s, n, k, v - 1, 0, ctypes.c_void_p(x.data_ptr()), 0, 9),
+                           1 << 20))
+        L.sfft_server_destroy(s)
+    s = _server(L, _lib, max_batch=2, budget=int(1.3 * (need[0] + need[1])))
+    order = [j for _ in range(12) for j in (0, 1)]
+    ids = [L.sfft_server_submit(s, shapes[j][0], shapes[j][1], shapes[j][2] - 1, 0,
+                                ctypes.c_void_p(xs[j].data_ptr()), 0, 9) for j in order]
+    got = [_wait(L, _lib, s, i, 1 << 20) for i in ids]
+    stats = (ctypes.c_long * 9)()
+    L.sfft_server_stats(s, stats, 9)
+    L.sfft_server_destroy(s)
+    for j, (gi, gv, _) in zip(order, got):
+        np.testing.assert_array_equal(gi, alone[j][0])
+        np.testing.assert_array_equal(gv, alone[j][1])
+    assert stats[5] <= stats[6]
