@@ -488,7 +488,15 @@ def stream_requests(nreq, seed=42):
     return out
 
 
-def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=0.8, seed=42):
+def stream_leg(L, _lib, local, precision, nreq, **kw):
+    """stream_leg_ with its time limit turned into an error entry."""
+    try:
+        return stream_leg_(L, _lib, local, precision, nreq, **kw)
+    except TimeoutError as e:
+        return {"error": str(e)}
+
+
+def stream_leg_(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=0.8, seed=42, limit_s=900):
     """The mixed stream through the continuous-batching server: plans are
     built once per (n, k bucket, version) and kept on the device under an
     HBM budget; a closed-loop burst measures capacity, then the requests
@@ -496,6 +504,7 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
     import threading
     import torch
     from sfft_gb300 import signals
+    t_start = time.perf_counter()
     reqs = stream_requests(nreq, seed)
     dev = torch.device("cuda", local)
     sig = {}
@@ -522,26 +531,52 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
     if not srv:
         return {"error": _lib.last_error()}
     lat = ctypes.c_double()
+    try:
+        return _stream_phases(L, srv, reqs, ptr, precision, nreq, load, seed, limit_s, lat, t_start, sig, voted,
+                              budget_gb)
+    finally:
+        L.sfft_server_destroy(srv)
+        sig.clear()
+        torch.cuda.empty_cache()
+
+
+def _stream_phases(L, srv, reqs, ptr, precision, nreq, load, seed, limit_s, lat, t_start, sig, voted, budget_gb):
+    import threading
+    sig_bytes = sum(x.numel() * x.element_size() for x in sig.values())
 
     def submit(i, seed_):
         n, k, version, c64 = reqs[i]
         return L.sfft_server_submit(srv, n, k, version - 1, precision, ptr[i], 1 if c64 else 0, seed_)
 
+    deadline = [time.perf_counter() + limit_s]
+
     def wait(rid):
-        c = L.sfft_server_wait(srv, rid, None, None, 0, ctypes.byref(lat))
+        # bounded: a stream that stops making progress ends the leg with an error
+        left_ms = 1e3 * (deadline[0] - time.perf_counter())
+        c = L.sfft_server_wait_for(srv, rid, None, None, 0, ctypes.byref(lat), max(1.0, left_ms))
+        if c == -2:
+            raise TimeoutError("serving stream made no progress within its time limit")
         return c, lat.value
 
+    def log(msg):
+        print(f"[stream {'fp32' if precision == 1 else 'fp64'}] {msg} ({time.perf_counter() - t_start:.0f} s)",
+              file=sys.stderr, flush=True)
+
+    log(f"{len(sig)} signals ({sig_bytes / 2**30:.1f} GiB) on the device")
     # plans: one request per distinct plan, outside the timed region
     t0 = time.perf_counter()
     first = {}
     for i, (n, k, version, c64) in enumerate(reqs):
         kk = L.sfft_tuned_k(k) if version == 2 else max(8, 1 << (max(k, 1) - 1).bit_length())
         first.setdefault((n, kk, version), i)
-    fails = 0
+    fails, errors = 0, set()
     for i in first.values():
         c, _ = wait(submit(i, i))
-        fails += c < 0
+        if c < 0:
+            fails += 1
+            errors.add(f"{reqs[i][:3]}: {L.sfft_last_error().decode()}")
     plan_s = time.perf_counter() - t0
+    log(f"{len(first)} plans built")
     # capacity: every request submitted at once
     burst = min(nreq, 2000)
     t0 = time.perf_counter()
@@ -549,6 +584,7 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
     for rid in ids:
         wait(rid)
     capacity = burst / (time.perf_counter() - t0)
+    log(f"burst of {burst}: {capacity:.0f} solves/s")
     # the timed stream
     rate = load * capacity
     gaps = np.random.default_rng(seed + 1).exponential(1.0 / rate, size=nreq)
@@ -566,7 +602,15 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
             failed[0] += c < 0
         done_t[0] = time.perf_counter()
 
-    th = threading.Thread(target=waiter)
+    err = []
+
+    def waiter_safe():
+        try:
+            waiter()
+        except TimeoutError as e:
+            err.append(str(e))
+
+    th = threading.Thread(target=waiter_safe)
     th.start()
     t0 = time.perf_counter()
     t_next = t0
@@ -576,18 +620,19 @@ def stream_leg(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=
             pass
         ids[i] = submit(i, 100000 + i)
     th.join()
+    log("stream done" if not err else err[0])
+    if err:
+        return {"error": err[0]}
     stats = (ctypes.c_long * 9)()
     L.sfft_server_stats(srv, stats, 9)
-    L.sfft_server_destroy(srv)
     by_v = {v: [lats[i] for i in range(nreq) if reqs[i][2] == v] for v in (2, 3)}
-    del sig
-    torch.cuda.empty_cache()
     return {"requests": nreq, "precision": "fp32" if precision == 1 else "fp64 (v3 always fp64)",
             "solves_per_s": nreq / (done_t[0] - t0), "offered_rate": rate, "capacity_burst_solves_per_s": capacity,
             "p50_ms": pct(lats, 50), "p99_ms": pct(lats, 99),
             "p50_ms_v2": pct(by_v[2], 50), "p99_ms_v2": pct(by_v[2], 99),
             "p50_ms_v3": pct(by_v[3], 50), "p99_ms_v3": pct(by_v[3], 99),
-            "failed": failed[0] + fails, "plans_built": len(first), "plan_build_s": plan_s,
+            "failed": failed[0], "plans_failed": fails, "plan_errors": sorted(errors)[:5],
+            "plans_built": len(first), "plan_build_s": plan_s,
             "batches": int(stats[0]), "plans_evicted": int(stats[2]), "deferred": int(stats[3]),
             "batches_spilled_to_host": int(stats[8]), "v2_mode": "voted" if voted else "reference (all comb candidates)",
             "hbm_budget_gb": budget_gb, "signal_pool_gb": sig_bytes / 2**30,

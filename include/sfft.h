@@ -228,6 +228,10 @@ long sfft_server_submit(sfft_server *s, int n, int k, enum sfft_version version,
  * values as complex128) and the submit-to-completion latency.  Returns the
  * number of coefficients, or -1. */
 long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val, long cap, double *latency_ms);
+/* As sfft_server_wait, giving up after timeout_ms (< 0: no limit): then
+ * returns -2 and the request stays pending. */
+long sfft_server_wait_for(sfft_server *s, long id, int *out_idx, complex_t *out_val, long cap, double *latency_ms,
+                          double timeout_ms);
 /* Device bytes the server reserves for a plan of this shape with
  * `max_batch` slots (its admission estimate), or -1. */
 long sfft_server_plan_bytes(int n, int k, enum sfft_version version, int precision, int max_batch);

@@ -487,6 +487,11 @@ long sfft_server_submit(sfft_server *s, int n, int k, enum sfft_version version,
 }
 
 long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val, long cap, double *latency_ms) {
+  return sfft_server_wait_for(s, id, out_idx, out_val, cap, latency_ms, -1.0);
+}
+
+long sfft_server_wait_for(sfft_server *s, long id, int *out_idx, complex_t *out_val, long cap, double *latency_ms,
+                          double timeout_ms) {
   if (!s) return -1;
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(id);
@@ -495,7 +500,14 @@ long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val,
     return -1;
   }
   Request *r = it->second;
-  while (!r->done.load(std::memory_order_acquire)) s->cv_done.wait_for(lk, std::chrono::microseconds(500));
+  const auto deadline = Clock::now() + std::chrono::microseconds((long)(1000.0 * std::max(0.0, timeout_ms)));
+  while (!r->done.load(std::memory_order_acquire)) {
+    if (timeout_ms >= 0 && Clock::now() >= deadline) {
+      sfft::set_last_error("timed out waiting for the request (it stays queued)");
+      return -2;
+    }
+    s->cv_done.wait_for(lk, std::chrono::microseconds(500));
+  }
   if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
   long result = -1;
   if (r->failed) {

@@ -225,6 +225,30 @@ __global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) {
 // f mod W is a comb residue); reaching the threshold appends f to the
 // hits (computefourier-1.0-2.0.cc:91-116, :125-184).  Counters carry the
 // exec's epoch in their upper 24 bits, so they never need clearing.
+// One vote for frequency f: the counter is (epoch << 8) | votes, so a
+// counter from an earlier execution restarts at 1.  The vote that reaches
+// the threshold records the frequency (v1, and v2 in the voted mode).
+__device__ __forceinline__ void vote_one(const V12Dev &d, int slot, unsigned f, unsigned ep, unsigned *score,
+                                         int *cnt) {
+  unsigned cur = score[f], nv;
+  for (;;) {
+    nv = ((cur >> 8) == ep) ? cur + 1u : ((ep << 8) | 1u);
+    const unsigned prev = atomicCAS(&score[f], cur, nv);
+    if (prev == cur) break;
+    cur = prev;
+  }
+  if ((int)(nv & 255u) == d.thresh) {
+    atomicAdd(&cnt[CNT_VOTED], 1);
+    if (d.version == 0 || d.voted) {
+      const int pos = atomicAdd(&cnt[CNT_HITS], 1);
+      if (pos < d.hit_cap)
+        d.hits[(long)slot * d.hit_cap + pos] = (int)f;
+      else
+        atomicOr(&cnt[CNT_ERR], ERR_HIT_OVERFLOW);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) k_vote(V12Dev d) {
   const int slot = blockIdx.y;
   const int q = d.q_loc, lq = dlog2(q);
@@ -251,23 +275,38 @@ __global__ void __launch_bounds__(256) k_vote(V12Dev d) {
       const unsigned r = f & (unsigned)(d.W - 1);
       if (!((bits[r >> 5] >> (r & 31)) & 1u)) return;
     }
-    unsigned cur = score[f], nv;
-    for (;;) {
-      nv = ((cur >> 8) == ep) ? cur + 1u : ((ep << 8) | 1u);
-      const unsigned prev = atomicCAS(&score[f], cur, nv);
-      if (prev == cur) break;
-      cur = prev;
-    }
-    if ((int)(nv & 255u) == d.thresh) {
-      atomicAdd(&cnt[CNT_VOTED], 1);
-      if (d.version == 0 || d.voted) {
-        const int pos = atomicAdd(&cnt[CNT_HITS], 1);
-        if (pos < d.hit_cap)
-          d.hits[(long)slot * d.hit_cap + pos] = (int)f;
-        else
-          atomicOr(&cnt[CNT_ERR], ERR_HIT_OVERFLOW);
-      }
-    }
+    vote_one(d, slot, f, ep, score, cnt);
+  }
+}
+
+// v2 voting by enumeration: for selected bucket J and comb residue r, the
+// positions p of J's range whose frequency p a mod n lies in residue class r
+// mod W are p = c (mod W) with c = r a^-1 mod W (a odd; W divides n) -- one
+// thread per (loop, bucket, residue) visits exactly those, instead of one
+// thread per position testing the residue bitmap.  Same votes, any order.
+__global__ void __launch_bounds__(256) k_vote_comb(V12Dev d, int cmax) {
+  const int slot = blockIdx.y;
+  const long per_loop = (long)d.num * cmax;
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= per_loop * d.L_loc) return;
+  const int j = (int)(g / per_loop);
+  const long e = g - (long)j * per_loop;
+  const int i = (int)(e / cmax), ri = (int)(e - (long)i * cmax);
+  int *cnt = d.counters + slot * CNT_STRIDE;
+  if (ri >= cnt[CNT_COMB]) return;
+  const unsigned r = (unsigned)d.comb_list[(long)slot * d.W + ri];
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const unsigned a = (unsigned)rp[j], ai = (unsigned)rp[d.L + j];
+  const unsigned ep = (unsigned)rp[2 * d.L + d.comb_loops];
+  const unsigned mask = (unsigned)d.n - 1u, wm = (unsigned)d.W - 1u;
+  const int q = d.q_loc;
+  const int J = d.J[((long)slot * d.L + j) * d.num + i];
+  const unsigned low = ((unsigned)J * (unsigned)q - (unsigned)(q >> 1) + (unsigned)d.n) & mask;
+  const unsigned c = (r * ai) & wm;
+  unsigned *score = d.score + (long)slot * d.n;
+  for (unsigned k = (c - low) & wm; k < (unsigned)q; k += (unsigned)d.W) {
+    const unsigned p = (low + k) & mask;
+    vote_one(d, slot, (p * a) & mask, ep, score, cnt);
   }
 }
 
@@ -948,6 +987,15 @@ static cudaError_t launch_estimate(const V12Dev &d, int nslots, cudaStream_t s) 
   return dispatch_estimate<k_estimate32_k>(d, nslots, sm_count(), s);
 }
 
+// v2 voting by enumeration is the default (SFFT_GB300_VOTE_ENUM=0 turns it off).
+static bool vote_enum() {
+  static const bool on = [] {
+    const char *e = getenv("SFFT_GB300_VOTE_ENUM");
+    return !e || atoi(e) != 0;
+  }();
+  return on;
+}
+
 // The split FP32 fold is the default (SFFT_GB300_FOLD_SPLIT=0 turns it off).
 static bool fold_split() {
   static const bool on = [] {
@@ -1006,8 +1054,14 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
     if ((e = cudaGetLastError())) return e;
   }
   {
-    const long votes = ((long)d.num * d.q_loc) * d.L_loc;
-    k_vote<<<dim3((unsigned)((votes + 255) / 256), nslots), 256, 0, s>>>(d);
+    const long cmax = std::min<long>(d.W, (long)d.comb_loops * d.num);
+    if (d.version == 1 && vote_enum() && cmax < d.q_loc) {
+      const long threads = (long)d.num * cmax * d.L_loc;
+      k_vote_comb<<<dim3((unsigned)((threads + 255) / 256), nslots), 256, 0, s>>>(d, (int)cmax);
+    } else {
+      const long votes = ((long)d.num * d.q_loc) * d.L_loc;
+      k_vote<<<dim3((unsigned)((votes + 255) / 256), nslots), 256, 0, s>>>(d);
+    }
     if ((e = cudaGetLastError())) return e;
     note_launches(1);
   }
