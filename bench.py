@@ -277,8 +277,8 @@ def gb300_arm(a, ws, rank, local):
 
     if a.only == "stream":
         if rank == 0:
-            print(json.dumps({"serving_stream_fp32": stream_leg(L, _lib, local, 1, a.stream_requests),
-                              "serving_stream_fp64": stream_leg(L, _lib, local, 0, a.stream_requests)}),
+            print(json.dumps({"serving_stream_fp32": stream_leg(L, _lib, local, 1, a.stream_requests, limit_s=700),
+                              "serving_stream_fp64": stream_leg(L, _lib, local, 0, a.stream_requests, limit_s=700)}),
                   flush=True)
         return
     if a.only == "uneven":
