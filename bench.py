@@ -45,7 +45,7 @@ def args_():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--pool", type=int, default=64)
-    ap.add_argument("--only", default="all", choices=["all", "device", "uneven", "stream"],
+    ap.add_argument("--only", default="all", choices=["all", "device", "uneven", "stream", "configs"],
                     help="device: only the device-resident timed legs (for profiler captures); "
                          "uneven: only the 256-signal uneven batch; stream: only the mixed serving stream")
     ap.add_argument("--stream-requests", type=int, default=10000, help="requests in the mixed serving stream")
@@ -277,9 +277,13 @@ def gb300_arm(a, ws, rank, local):
 
     if a.only == "stream":
         if rank == 0:
-            print(json.dumps({"serving_stream_fp32": stream_leg(L, _lib, local, 1, a.stream_requests, limit_s=700),
-                              "serving_stream_fp64": stream_leg(L, _lib, local, 0, a.stream_requests, limit_s=700)}),
+            print(json.dumps({"serving_stream_fp32": stream_leg(L, _lib, local, 1, a.stream_requests, limit_s=480),
+                              "serving_stream_fp64": stream_leg(L, _lib, local, 0, a.stream_requests, limit_s=480)}),
                   flush=True)
+        return
+    if a.only == "configs":
+        if rank == 0:
+            print(json.dumps({"other_configs": configs_leg(L, _lib, local)}), flush=True)
         return
     if a.only == "uneven":
         if rank == 0:
@@ -330,8 +334,8 @@ def gb300_arm(a, ws, rank, local):
     lat32, lat64 = lat(p32, oval32), lat(p64, oval64)
 
     # ---- serving: Poisson arrivals at 80% of each form's batched throughput
-    serve32 = serving_leg(L, _lib, pool, 1, 0.8 * value / ws, 4000, local)
-    serve64 = serving_leg(L, _lib, pool, 0, 0.8 * value64 / ws, 1500, local)
+    serve32 = serving_leg(L, _lib, pool, 1, 0.8, 4000, local)
+    serve64 = serving_leg(L, _lib, pool, 0, 0.8, 1500, local)
 
     # ---- accuracy: FP32 vs FP64 on the same draws, and both vs the truth
     acc = accuracy(p32, p64, signals, p32v)
@@ -344,6 +348,8 @@ def gb300_arm(a, ws, rank, local):
 
     # ---- 256 signals of uneven (n, k) as one CUDA graph
     uneven = uneven_leg(L, _lib, local)
+    # ---- the other named configurations (C1 v1, C2 v3)
+    other = configs_leg(L, _lib, local)
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": a.steps,
@@ -352,7 +358,7 @@ def gb300_arm(a, ws, rank, local):
         "config": config(a),
         "p50_ms": serve32["p50_ms"], "p99_ms": serve32["p99_ms"],
         "latency_basis": "submit-to-completion of requests arriving as a Poisson process at 80% of the "
-                         "batched throughput, through the continuous-batching server (sfft_server_*)",
+                         "server's burst capacity, through the continuous-batching server (sfft_server_*)",
         "serving": {"fp32": serve32, "fp64": serve64},
         "batch_step_ms": {"p50": pct(per32, 50), "p99": pct(per32, 99)},
         "fp64": {"value": value64, "unit": "solves/s", "ms_per_step": t64max / s64,
@@ -374,6 +380,7 @@ def gb300_arm(a, ws, rank, local):
         "stage_ms_per_launch_fp64": stage_table(st64),
         "e2e": e2e,
         "uneven_batch": uneven,
+        "other_configs": other,
         "gpu_launches": launches32,
         "clocks": clocks,
     }
@@ -385,6 +392,71 @@ def gb300_arm(a, ws, rank, local):
                                           "OpenMP over signals"}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def configs_leg(L, _lib, local, reps=20):
+    """The other named configurations, FP64 (their plain form): C1 v1
+    n = 2^16, k = 50 and C2 v3 n = 2^24, k = 1000, noiseless |X| = 1: batched
+    throughput, single-request latency and recovery against the truth."""
+    import torch
+    from sfft_gb300 import signals
+    out = {}
+    for name, n, k, ver, batch, seed in (("C1_v1_n65536_k50", 1 << 16, 50, 0, 64, 0),
+                                         ("C2_v3_n16777216_k1000", 1 << 24, 1000, 2, 4, 1)):
+        sig = [signals.make_signal_torch(n, k, seed + s, device=torch.device("cuda", local)) for s in range(batch)]
+        o = _lib.Options(0, local, batch)
+        p = L.sfft_make_plan_ex(n, k, ver, 0, ctypes.byref(o))
+        if not p:
+            out[name] = {"error": _lib_err(L)}
+            continue
+        cap = L.sfft_output_capacity(p)
+        idx = torch.empty((batch, cap), dtype=torch.int32, device=sig[0][0].device)
+        val = torch.empty((batch, cap), dtype=torch.complex128, device=sig[0][0].device)
+        cnt = torch.zeros(batch, dtype=torch.int32, device=sig[0][0].device)
+        stream = torch.cuda.ExternalStream(L.sfft_plan_stream(p))
+        ins = (ctypes.c_void_p * batch)(*[x.data_ptr() for x, _, _ in sig])
+        seeds = (ctypes.c_uint * batch)(*range(batch))
+
+        def run(m):
+            if L.sfft_exec_batch_ex(p, m, ins, 0, seeds, ctypes.c_void_p(idx.data_ptr()),
+                                    ctypes.c_void_p(val.data_ptr()), ctypes.c_void_p(cnt.data_ptr()), cap, None):
+                raise RuntimeError(_lib_err(L))
+
+        def timed(m):
+            ts = []
+            for i in range(reps + 3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                run(m)
+                e1.record(stream)
+                e1.synchronize()
+                if i >= 3:
+                    ts.append(e0.elapsed_time(e1))
+            return ts
+
+        tb, t1 = timed(batch), timed(1)
+        run(batch)
+        L.sfft_sync(p)
+        missed = spurious = 0
+        worst = 0.0
+        for s in range(batch):
+            c = int(cnt[s])
+            est = np.zeros(n, dtype=np.complex128)
+            v = val[s, :c].cpu().numpy()
+            est[idx[s, :c].cpu().numpy()] = np.conj(v) if ver < 2 else v
+            _, pos, vals = sig[s]
+            err = np.abs(est[pos] - vals)
+            worst = max(worst, float(err.max()))
+            missed += int(np.count_nonzero(err > 0.5))
+            est[pos] = 0
+            spurious += int(np.count_nonzero(np.abs(est) > 0.5))
+        L.sfft_free_plan(p)
+        out[name] = {"solves_per_s": batch / (1e-3 * float(np.median(tb))), "batch": batch,
+                     "batch_ms_p50": pct(tb, 50), "single_ms_p50": pct(t1, 50), "single_ms_p99": pct(t1, 99),
+                     "missed": missed, "spurious": spurious, "worst_tone_error": worst, "precision": "fp64"}
+        del sig
+        torch.cuda.empty_cache()
+    return out
 
 
 def uneven_shapes(count=256):
@@ -618,6 +690,10 @@ def _stream_phases(L, srv, reqs, ptr, precision, nreq, load, seed, limit_s, lat,
         t_next += gaps[i]
         while time.perf_counter() < t_next:
             pass
+        if time.perf_counter() > deadline[0] or err:  # out of time: stop offering load
+            for j in range(i, nreq):
+                ids[j] = -1
+            break
         ids[i] = submit(i, 100000 + i)
     th.join()
     log("stream done" if not err else err[0])
@@ -642,10 +718,11 @@ def _stream_phases(L, srv, reqs, ptr, precision, nreq, load, seed, limit_s, lat,
                         "up to a power of two (at least 8)"}
 
 
-def serving_leg(L, _lib, pool, precision, rate, nreq, device):
-    """Requests of the bench workload submitted at Poisson times (rate per
-    second) to a continuous-batching server; latency = submit to completion
-    on the device."""
+def serving_leg(L, _lib, pool, precision, load, nreq, device):
+    """Requests of the bench workload submitted at Poisson times to a
+    continuous-batching server, at `load` times the server's own capacity
+    (measured first with every request of a burst submitted at once);
+    latency = submit to completion on the device."""
     import threading
     opts = _lib.ServerOptions(device, 32, 0, 0, 0)
     srv = L.sfft_server_create(ctypes.byref(opts))
@@ -658,6 +735,14 @@ def serving_leg(L, _lib, pool, precision, rate, nreq, device):
             for i in range(64)]
     for w in warm:
         L.sfft_server_wait(srv, w, None, None, 0, ctypes.byref(lat))
+    burst = min(nreq, 2000)
+    t0 = time.perf_counter()
+    ids = [L.sfft_server_submit(srv, N_SIG, K_SIG, VERSION - 1, precision, ptrs[i % len(ptrs)], 0, 500 + i)
+           for i in range(burst)]
+    for rid in ids:
+        L.sfft_server_wait(srv, rid, None, None, 0, ctypes.byref(lat))
+    capacity = burst / (time.perf_counter() - t0)
+    rate = load * capacity
     rng = np.random.default_rng(SEED)
     gaps = rng.exponential(1.0 / rate, size=nreq)
     ids = [None] * nreq
@@ -687,7 +772,8 @@ def serving_leg(L, _lib, pool, precision, rate, nreq, device):
     stats = (ctypes.c_long * 8)()
     L.sfft_server_stats(srv, stats, 8)
     L.sfft_server_destroy(srv)
-    return {"offered_rate": rate, "requests": nreq, "solves_per_s": nreq / (done_t[0] - t0),
+    return {"offered_rate": rate, "capacity_burst_solves_per_s": capacity, "load": load, "requests": nreq,
+            "solves_per_s": nreq / (done_t[0] - t0),
             "p50_ms": pct(lats, 50), "p99_ms": pct(lats, 99), "batches": int(stats[0]),
             "precision": "fp32" if precision == 1 else "fp64"}
 

@@ -276,6 +276,15 @@ void sfft_mixed_destroy(sfft_mixed *m);
  * Call between executions; the output capacity may change.  0 or -1. */
 int sfft_plan_v2_voted(sfft_plan *plan, int on);
 
+/* ---- self-test (no counterpart in the reference) ----------------------- */
+
+/* The FP64 estimation divides through a host reciprocal with an exact
+ * certificate (falling back to IEEE division).  This runs it against the
+ * IEEE division on `count` pseudo-random operand pairs (exponents within
+ * +-span) on the current device; returns the number of disagreements (0
+ * expected) and stores how many the fast path certified. */
+long sfft_selftest_division(unsigned long long seed, long count, int span, long *certified);
+
 /* ---- constants chosen by this project (no counterpart in the reference) */
 
 /* v1/v2 constants for (n, k): the autotuner's table row for n and the k

@@ -227,7 +227,7 @@ def main():
     ap.add_argument("--logn", default="16-22", help="range of log2 n, e.g. 16-22")
     ap.add_argument("--kb", default="16,32,64,128,256,512", help="k buckets")
     ap.add_argument("--batch", type=int, default=16)
-    ap.add_argument("--nacc", type=int, default=3, help="signals checked for accuracy")
+    ap.add_argument("--nacc", type=int, default=6, help="signals checked for accuracy")
     ap.add_argument("--rounds", type=int, default=3)
     ap.add_argument("--out-dir", default=".")
     ap.add_argument("--from-table", action="store_true", help="start from the compiled table's rows")

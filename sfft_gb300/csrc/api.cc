@@ -253,7 +253,7 @@ bool upload_v12_window(DBuf &b, const std::vector<double> &freq, int n, int q, i
       w[4 * m] = c;
       w[4 * m + 1] = dd;
       w[4 * m + 2] = c * c + dd * dd;  // same rounding as the reference's hadd
-      w[4 * m + 3] = 0.0;
+      w[4 * m + 3] = w[4 * m + 2] != 0.0 ? 1.0 / w[4 * m + 2] : 0.0;  // RN(1/den) for div_rn_rcp
     }
     return b.upload(w);
   }
@@ -298,12 +298,22 @@ bool ensure_slots(PlanImpl &P, int want) {
     const int L = L12(P);
     P.rp_stride = 2 * L + p.Comb_loops + 1;
     const int q = P.n / p.B_loc;
-    P.hit_cap = P.version == 0 || P.voted
+    P.hit_cap = P.version == 0
                     ? (int)std::min<long>((long)P.n, ((long)p.loops_loc * p.B_thresh * q) / p.loops_thresh + 1)
                     : 1;
     const long comb_max = std::min<long>((long)p.W_Comb, (long)p.Comb_loops * p.B_thresh);
     P.out_cap = P.version == 0 ? P.hit_cap : (int)(comb_max * (P.n / p.W_Comb));
-    if (P.voted) P.out_cap = std::max(P.out_cap, P.hit_cap);
+    if (P.voted) {
+      // voted v2: a candidate needs `thresh` votes; at most min(comb
+      // candidates, loc_loops * 2k * n/B / thresh) can reach it, but a signal
+      // with k tones brings about k of them plus a few collisions.  The list
+      // holds max(65536, 8 * 2k); a longer one sets ERR_HIT_OVERFLOW and the
+      // execution reports an error (nothing is dropped silently).
+      const long vote_max = ((long)p.loops_loc * p.B_thresh * q) / p.loops_thresh + 1;
+      P.hit_cap = (int)std::min<long>(std::min<long>((long)P.out_cap, vote_max),
+                                      std::max<long>(65536, 8L * p.B_thresh));
+      P.out_cap = P.hit_cap;
+    }
     if (P.prec == sfft::PREC_FP64 && !P.xs32.ensure(8 * p.x_samp_size * S)) return false;
     if (P.large_b && !P.xs_tmp.ensure(cs * p.x_samp_size * S)) return false;
     if (P.large_c && (!P.comb_buf.ensure(cs * (size_t)p.Comb_loops * p.W_Comb * S) ||
@@ -466,6 +476,11 @@ sfft::V12Dev v12_view(PlanImpl &P) {
   d.hit_cap = P.hit_cap;
   d.out_cap = P.out_cap;
   d.voted = P.voted;
+  static const int div_rcp = [] {
+    const char *e = getenv("SFFT_GB300_DIV_RCP");
+    return e ? atoi(e) : 1;
+  }();
+  d.div_rcp = div_rcp;
   d.out_stride = P.out_cap;
   d.rparams = P.rparams.as<int>();
   d.rp_stride = P.rp_stride;
@@ -1135,6 +1150,14 @@ int sfft_plan_v2_voted(sfft_plan *plan, int on) {
   const int slots = P->slots;
   P->slots = 0;  // re-derive capacities and grow the buffers they need
   return ensure_slots(*P, std::max(1, slots)) ? 0 : -1;
+}
+
+long sfft_selftest_division(unsigned long long seed, long count, int span, long *certified) {
+  unsigned long long out[2] = {0, 0};
+  if (count < 1 || span < 1 || span > 1000 || !cuda_ok(sfft::div_selftest(seed, count, span, out), "selftest"))
+    return -1;
+  if (certified) *certified = (long)out[1];
+  return (long)out[0];
 }
 
 long sfft_output_capacity(const sfft_plan *plan) {

@@ -60,6 +60,7 @@ struct V12Dev {
   int *out_count;           // optional: per-slot coefficient count
   int hit_cap, out_cap;
   int voted;                // v2: estimate only candidates that reached the vote threshold
+  int div_rcp;              // FP64 divisions via the host reciprocal + certificate (div_rn_rcp)
   long out_stride;
   // per-exec inputs
   const int *rparams;       // per slot: a[L], ai[L], comb_offsets[comb_loops], epoch
@@ -119,6 +120,9 @@ struct V3Dev {
 cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t stream, StageEvents *se = nullptr);
 // Largest FP64 FFT the v3 filter kernel runs in shared memory.
 int v3_max_smem_fft();
+// div_rn_rcp against __ddiv_rn on `count` pseudo-random operand pairs:
+// out[0] disagreements, out[1] results the fast path certified.
+cudaError_t div_selftest(unsigned long long seed, long count, int span, unsigned long long *out);
 // Batched complex128 FFTs of length N in global memory (the same stages as
 // the shared-memory FFT): narr arrays per slot, arr_stride apart, slots
 // slot_stride apart; b is scratch of the same shape; result in a.

@@ -210,25 +210,24 @@ bool spill_batch(sfft_server *s, Batch *b) {
   return true;
 }
 
-// Makes `need` more bytes fit the budget: evicts idle plans (least recently
-// used first, never `keep`), then spills finished batches' results to host
-// memory (oldest first).
+// Makes `need` more bytes fit the budget: first moves finished batches'
+// results to host memory (oldest first; cheap to undo), then evicts idle
+// plans (least recently used first, never `keep`; rebuilding a large plan
+// takes seconds).
 bool make_room(sfft_server *s, long need, const PlanEntry *keep = nullptr) {
   while (s->held + need > s->budget) {
+    Batch *sp = nullptr;
+    for (Batch *b : s->batches)
+      if (!b->spilled && b->complete.load(std::memory_order_acquire)) {
+        sp = b;
+        break;
+      }
+    if (sp && spill_batch(s, sp)) continue;
     PlanEntry *victim = nullptr;
     for (auto &kv : s->plans)
       if (kv.second != keep && !kv.second->busy.load() && (!victim || kv.second->last_used < victim->last_used))
         victim = kv.second;
-    if (!victim) {
-      Batch *sp = nullptr;
-      for (Batch *b : s->batches)
-        if (!b->spilled && b->complete.load(std::memory_order_acquire)) {
-          sp = b;
-          break;
-        }
-      if (!sp || !spill_batch(s, sp)) return false;
-      continue;
-    }
+    if (!victim) return false;
     s->held -= victim->bytes;
     sfft_free_plan(victim->plan);
     s->plans.erase(victim->key);

@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256) k_vote_comb(V12Dev d, int cmax) {
 // ---------------------------------------------------------------- bucket --
 
 template <typename R, int PER>
-__global__ void __launch_bounds__(1024) k_bucket(V12Dev d) {
+__global__ void __launch_bounds__(1024, (sizeof(R) == 4 && PER == 1) ? 2 : 1) k_bucket(V12Dev d) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int j = blockIdx.x, slot = blockIdx.y;
   const bool loc = j < d.L_loc;
@@ -635,10 +635,11 @@ __device__ __forceinline__ double2 value64(const V12Dev &d, const double2 *xs, i
   const double2 v = xs[s.off + hashed];
   const double2 *wp = (const double2 *)(j < d.L_loc ? d.win_loc : d.win_est) + 2 * m;
   const double2 h = __ldg(wp);
-  const double den = __ldg(wp + 1).x;
+  const double2 dr = __ldg(wp + 1);  // (c^2 + d^2, its rounded reciprocal)
   using A = Ar<double>;
-  return make_double2(A::div(A::add(A::mul(v.x, h.x), A::mul(v.y, h.y)), den),
-                      A::div(A::sub(A::mul(v.x, h.y), A::mul(v.y, h.x)), den));
+  const double nr = A::add(A::mul(v.x, h.x), A::mul(v.y, h.y)), ni = A::sub(A::mul(v.x, h.y), A::mul(v.y, h.x));
+  if (d.div_rcp) return make_double2(div_rn_rcp(nr, dr.x, dr.y), div_rn_rcp(ni, dr.x, dr.y));
+  return make_double2(A::div(nr, dr.x), A::div(ni, dr.x));
 }
 
 // Exact lower medians of all L FP64 values (used when the FP32 pre-selection
@@ -1070,6 +1071,46 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
   mark(se, s);
   note_launches(3);
   return cudaSuccess;
+}
+
+// Self-test of div_rn_rcp against __ddiv_rn on pseudo-random operands
+// (splitmix64 bits: random signs, mantissas and exponents spread over
+// [2^-lo, 2^hi)); counts disagreements and fast-path hits.
+__global__ void k_div_selftest(unsigned long long seed, long count, int span, unsigned long long *out) {
+  unsigned long long bad = 0, fast = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
+    auto mix = [](unsigned long long z) {
+      z += 0x9E3779B97F4A7C15ull;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      return z ^ (z >> 31);
+    };
+    const unsigned long long a = mix(seed + 2 * (unsigned long long)i), b = mix(seed + 2 * (unsigned long long)i + 1);
+    const int ea = 1023 + (int)((a >> 52) % (unsigned)(2 * span + 1)) - span;
+    const int eb = 1023 + (int)((b >> 52) % (unsigned)(2 * span + 1)) - span;
+    const double num = __longlong_as_double((long long)(((a >> 11) & 1ull) << 63 | (unsigned long long)ea << 52 |
+                                                        (a & 0xfffffffffffffull)));
+    const double den = __longlong_as_double((long long)((unsigned long long)eb << 52 | (b & 0xfffffffffffffull)));
+    const double r = __drcp_rn(den);
+    const double q = div_rn_rcp(num, den, r), ref = __ddiv_rn(num, den);
+    bad += __double_as_longlong(q) != __double_as_longlong(ref);
+    const double q0 = __dmul_rn(num, r);
+    fast += __double_as_longlong(__fma_rn(__fma_rn(-q0, den, num), r, q0)) == __double_as_longlong(q);
+  }
+  atomicAdd(&out[0], bad);
+  atomicAdd(&out[1], fast);
+}
+
+cudaError_t div_selftest(unsigned long long seed, long count, int span, unsigned long long *host_out) {
+  unsigned long long *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 2 * sizeof(unsigned long long));
+  if (e) return e;
+  cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+  k_div_selftest<<<sm_count() * 8, 256>>>(seed, count, span, d);
+  e = cudaGetLastError();
+  if (!e) e = cudaMemcpy(host_out, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e;
 }
 
 cudaError_t global_fft_c128(void *a, void *b, int N, int narr, long arr_stride, long slot_stride, int nslots,
