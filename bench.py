@@ -277,8 +277,8 @@ def gb300_arm(a, ws, rank, local):
 
     if a.only == "stream":
         if rank == 0:
-            print(json.dumps({"serving_stream_fp32": stream_leg(L, _lib, local, 1, a.stream_requests, limit_s=480),
-                              "serving_stream_fp64": stream_leg(L, _lib, local, 0, a.stream_requests, limit_s=480)}),
+            print(json.dumps({"serving_stream_fp32": stream_leg(L, _lib, local, 1, a.stream_requests, limit_s=420),
+                              "serving_stream_fp64": stream_leg(L, _lib, local, 0, a.stream_requests, limit_s=300)}),
                   flush=True)
         return
     if a.only == "configs":
@@ -568,7 +568,7 @@ def stream_leg(L, _lib, local, precision, nreq, **kw):
         return {"error": str(e)}
 
 
-def stream_leg_(L, _lib, local, precision, nreq, budget_gb=96, max_batch=8, load=0.8, seed=42, limit_s=900):
+def stream_leg_(L, _lib, local, precision, nreq, budget_gb=160, max_batch=8, load=0.8, seed=42, limit_s=900):
     """The mixed stream through the continuous-batching server: plans are
     built once per (n, k bucket, version) and kept on the device under an
     HBM budget; a closed-loop burst measures capacity, then the requests

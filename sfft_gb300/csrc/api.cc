@@ -1148,7 +1148,10 @@ int sfft_plan_v2_voted(sfft_plan *plan, int on) {
     return -1;
   P->voted = on ? 1 : 0;
   const int slots = P->slots;
-  P->slots = 0;  // re-derive capacities and grow the buffers they need
+  P->slots = 0;  // re-derive capacities; the output and hit buffers are resized
+  P->out_idx.release();
+  P->out_val.release();
+  P->hits.release();
   return ensure_slots(*P, std::max(1, slots)) ? 0 : -1;
 }
 

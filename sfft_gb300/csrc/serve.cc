@@ -288,7 +288,7 @@ PlanEntry *get_plan(sfft_server *s, const PlanKey &key, std::string &err) {
   pe->key = key;
   pe->plan = p;
   pe->cap = sfft_output_capacity(p);
-  pe->bytes = std::max(need, sfft_plan_footprint(p));
+  pe->bytes = sfft_plan_footprint(p);  // what the plan holds (the estimate only admitted it)
   pe->tuned = tuned;
   pe->stream = (cudaStream_t)sfft_plan_stream(p);
   s->plans[key] = pe;
@@ -520,7 +520,7 @@ long sfft_server_wait_for(sfft_server *s, long id, int *out_idx, complex_t *out_
       cnt = (int)b->h_idx[r->slot].size();
     else
       ok = cudaMemcpy(&cnt, b->d_cnt + r->slot, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
-    if (ok && cnt > cap) {
+    if (ok && (out_idx || out_val) && cnt > cap) {  // no buffers: only the count is asked for
       sfft::set_last_error("output capacity too small");
       ok = false;
     }
