@@ -96,7 +96,9 @@ def test_small_budget_evicts_and_defers(env):
     shapes = [(1 << 16, 50, 2), (1 << 17, 50, 2), (1 << 18, 50, 1)]
     xs = [torch.from_numpy(signals.make_signal(n, k, 9)[0]).cuda() for n, k, _ in shapes]
     need = max(L.sfft_server_plan_bytes(n, k, v - 1, 0, 2) for n, k, v in shapes)
-    s = _server(L, _lib, max_batch=2, budget=int(1.5 * need))   # one plan (and its batch) at a time
+    # just above the largest admission estimate: a cached plan (charged its
+    # actual footprint) plus the next plan's estimate never fit together
+    s = _server(L, _lib, max_batch=2, budget=int(1.05 * need))
     ids = [L.sfft_server_submit(s, n, k, v - 1, 0, ctypes.c_void_p(x.data_ptr()), 0, 3)
            for rep in range(2) for (n, k, v), x in zip(shapes, xs)]
     counts = [_wait(L, _lib, s, i, 1 << 20)[0].size for i in ids]
