@@ -169,7 +169,9 @@ int sfft_sync(sfft_plan *plan);
  * what: 0 permutations a[L] then ai[L] (int); 1 selected buckets J[L][2k]
  * (int); 2 vote counts (n int); 3 bucket values x_samp (complex, plan
  * precision); 4 v2 comb residues (int, count returned); 5 v3 rounds;
- * 6 v3 estimates as (round, stage, frequency, re, im) doubles.
+ * 6 v3 estimates as (round, stage, frequency, re, im) doubles;
+ * 7 the 16 counters of slot 0 (0 hits, 1 comb residues, 2 outputs, 3 error
+ * bits, 4 voted, 8 FP64 medians that took the all-exact path).
  * Returns the number of elements written, or -1. */
 long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap);
 
@@ -275,15 +277,6 @@ void sfft_mixed_destroy(sfft_mixed *m);
  * tones are the same; the result is not the reference's output list.
  * Call between executions; the output capacity may change.  0 or -1. */
 int sfft_plan_v2_voted(sfft_plan *plan, int on);
-
-/* ---- self-test (no counterpart in the reference) ----------------------- */
-
-/* The FP64 estimation divides through a host reciprocal with an exact
- * certificate (falling back to IEEE division).  This runs it against the
- * IEEE division on `count` pseudo-random operand pairs (exponents within
- * +-span) on the current device; returns the number of disagreements (0
- * expected) and stores how many the fast path certified. */
-long sfft_selftest_division(unsigned long long seed, long count, int span, long *certified);
 
 /* ---- constants chosen by this project (no counterpart in the reference) */
 

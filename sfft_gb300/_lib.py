@@ -112,8 +112,6 @@ def load(build_if_missing=False):
     L.sfft_server_wait_for.argtypes = L.sfft_server_wait.argtypes + [ctypes.c_double]
     L.sfft_describe_plan_params.restype = ci
     L.sfft_describe_plan_params.argtypes = [ci, ci, ci, ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_long), ci]
-    L.sfft_selftest_division.restype = cl
-    L.sfft_selftest_division.argtypes = [ctypes.c_ulonglong, cl, ci, ctypes.POINTER(cl)]
     L.sfft_plan_v2_voted.restype = ci
     L.sfft_plan_v2_voted.argtypes = [PP, ci]
     L.sfft_tuned_params.restype = ci

@@ -253,7 +253,7 @@ bool upload_v12_window(DBuf &b, const std::vector<double> &freq, int n, int q, i
       w[4 * m] = c;
       w[4 * m + 1] = dd;
       w[4 * m + 2] = c * c + dd * dd;  // same rounding as the reference's hadd
-      w[4 * m + 3] = w[4 * m + 2] != 0.0 ? 1.0 / w[4 * m + 2] : 0.0;  // RN(1/den) for div_rn_rcp
+      w[4 * m + 3] = 0.0;
     }
     return b.upload(w);
   }
@@ -476,11 +476,7 @@ sfft::V12Dev v12_view(PlanImpl &P) {
   d.hit_cap = P.hit_cap;
   d.out_cap = P.out_cap;
   d.voted = P.voted;
-  static const int div_rcp = [] {
-    const char *e = getenv("SFFT_GB300_DIV_RCP");
-    return e ? atoi(e) : 1;
-  }();
-  d.div_rcp = div_rcp;
+
   d.out_stride = P.out_cap;
   d.rparams = P.rparams.as<int>();
   d.rp_stride = P.rp_stride;
@@ -1155,14 +1151,6 @@ int sfft_plan_v2_voted(sfft_plan *plan, int on) {
   return ensure_slots(*P, std::max(1, slots)) ? 0 : -1;
 }
 
-long sfft_selftest_division(unsigned long long seed, long count, int span, long *certified) {
-  unsigned long long out[2] = {0, 0};
-  if (count < 1 || span < 1 || span > 1000 || !cuda_ok(sfft::div_selftest(seed, count, span, out), "selftest"))
-    return -1;
-  if (certified) *certified = (long)out[1];
-  return (long)out[0];
-}
-
 long sfft_output_capacity(const sfft_plan *plan) {
   const PlanImpl *P = plan ? (const PlanImpl *)plan->data : nullptr;
   if (!P) {
@@ -1305,6 +1293,12 @@ long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap) {
   }
   std::lock_guard<std::mutex> g(P->mu);
   if (!cuda_ok(cudaStreamSynchronize(P->stream), "sync")) return -1;
+  if (what == 7) {  // the counters of batch slot 0, any version
+    if (cap < sfft::CNT_STRIDE) return -1;
+    if (!cuda_ok(cudaMemcpy(dst, P->counters.p, sizeof(int) * sfft::CNT_STRIDE, cudaMemcpyDeviceToHost), "debug"))
+      return -1;
+    return sfft::CNT_STRIDE;
+  }
   auto fetch = [&](const void *src, long count, size_t esz) -> long {
     if (count > cap) {
       set_err("debug buffer too small");

@@ -39,30 +39,6 @@ template <> struct Ar<double> {
   static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
 };
 
-// Correctly rounded num / den -- the IEEE quotient, as __ddiv_rn returns it
-// -- from r = RN(1/den) computed once on the host: q0 = RN(num r), one
-// Newton-Raphson correction q = RN(q0 + r (num - q0 den)) (Markstein's
-// division, IBM J. Res. Dev. 34(1), 1990), then a certificate: the FMA
-// remainder rem = RN(num - q den) is compared with t = den ulp(q) / 2.
-// Rounding is monotonic and t is representable, so |rem| < t implies
-// |num - q den| < t, i.e. |num / den - q| < ulp(q) / 2: q is the rounded
-// quotient.  Ties, q a power of two (its lower neighbour is closer),
-// zero / subnormal / huge operands and results, and every case the
-// certificate misses take __ddiv_rn, so the result is always the IEEE one.
-__device__ __forceinline__ double div_rn_rcp(double num, double den, double r) {
-  const double q0 = __dmul_rn(num, r);
-  const double q = __fma_rn(__fma_rn(-q0, den, num), r, q0);
-  const long long qb = __double_as_longlong(q);
-  const int E = (int)((qb >> 52) & 0x7ff);
-  const int Ed = (int)((__double_as_longlong(den) >> 52) & 0x7ff);
-  if (E > 54 && E < 2047 && (qb & 0xfffffffffffffLL) != 0 && den > 0.0 && Ed > 0 && Ed < 2047) {
-    const double rem = __fma_rn(-q, den, num);
-    const double t = __dmul_rn(den, __longlong_as_double((long long)(E - 53) << 52));  // den * ulp(q) / 2
-    if (t >= 2.2250738585072014e-308 && t <= 1.7976931348623157e308 && fabs(rem) < t) return q;
-  }
-  return __ddiv_rn(num, den);
-}
-
 template <> struct Ar<float> {
   static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
   static __device__ __forceinline__ float add(float a, float b) { return a + b; }

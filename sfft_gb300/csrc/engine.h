@@ -23,7 +23,7 @@ enum InType { IN_C128 = 0, IN_C64 = 1 };
 
 // Per-slot counters (one block of ints per slot, zeroed before each exec).
 enum Counter { CNT_HITS = 0, CNT_COMB = 1, CNT_OUT = 2, CNT_ERR = 3, CNT_VOTED = 4, CNT_V3 = 5,
-               CNT_TRACE = 6, CNT_EST = 7, CNT_STRIDE = 16 };
+               CNT_TRACE = 6, CNT_EST = 7, CNT_EXACT = 8, CNT_STRIDE = 16 };
 
 // Error bits reported in counters[CNT_ERR].
 enum ErrBits { ERR_HIT_OVERFLOW = 1, ERR_OUT_OVERFLOW = 2, ERR_V3_NOCONVERGE = 4, ERR_V3_CAP = 8 };
@@ -60,7 +60,6 @@ struct V12Dev {
   int *out_count;           // optional: per-slot coefficient count
   int hit_cap, out_cap;
   int voted;                // v2: estimate only candidates that reached the vote threshold
-  int div_rcp;              // FP64 divisions via the host reciprocal + certificate (div_rn_rcp)
   long out_stride;
   // per-exec inputs
   const int *rparams;       // per slot: a[L], ai[L], comb_offsets[comb_loops], epoch
@@ -120,9 +119,6 @@ struct V3Dev {
 cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t stream, StageEvents *se = nullptr);
 // Largest FP64 FFT the v3 filter kernel runs in shared memory.
 int v3_max_smem_fft();
-// div_rn_rcp against __ddiv_rn on `count` pseudo-random operand pairs:
-// out[0] disagreements, out[1] results the fast path certified.
-cudaError_t div_selftest(unsigned long long seed, long count, int span, unsigned long long *out);
 // Batched complex128 FFTs of length N in global memory (the same stages as
 // the shared-memory FFT): narr arrays per slot, arr_stride apart, slots
 // slot_stride apart; b is scratch of the same shape; result in a.

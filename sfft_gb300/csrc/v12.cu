@@ -635,11 +635,10 @@ __device__ __forceinline__ double2 value64(const V12Dev &d, const double2 *xs, i
   const double2 v = xs[s.off + hashed];
   const double2 *wp = (const double2 *)(j < d.L_loc ? d.win_loc : d.win_est) + 2 * m;
   const double2 h = __ldg(wp);
-  const double2 dr = __ldg(wp + 1);  // (c^2 + d^2, its rounded reciprocal)
+  const double den = __ldg(wp + 1).x;
   using A = Ar<double>;
-  const double nr = A::add(A::mul(v.x, h.x), A::mul(v.y, h.y)), ni = A::sub(A::mul(v.x, h.y), A::mul(v.y, h.x));
-  if (d.div_rcp) return make_double2(div_rn_rcp(nr, dr.x, dr.y), div_rn_rcp(ni, dr.x, dr.y));
-  return make_double2(A::div(nr, dr.x), A::div(ni, dr.x));
+  return make_double2(A::div(A::add(A::mul(v.x, h.x), A::mul(v.y, h.y)), den),
+                      A::div(A::sub(A::mul(v.x, h.y), A::mul(v.y, h.x)), den));
 }
 
 // Exact lower medians of all L FP64 values (used when the FP32 pre-selection
@@ -707,26 +706,34 @@ __device__ __forceinline__ bool candidate(const V12Dev &d, int slot, long h, uns
   return true;
 }
 
-// Picks the lower-median element of v[0..Lr) (FP32 approximations whose
-// exact values lie within +-e); returns its index if it is provably the
-// exact median, else -1.
+// Picks the lower-median element of v[0..Lr): FP32 approximations whose
+// exact values lie within +-e[j] of v[j].  Returns its index if it is
+// provably the exact lower median -- exactly m = (Lr-1)/2 intervals lie
+// wholly below its interval and Lr-1-m wholly above -- else -1.
+// Per-element bounds matter on clean signals: most candidates' values are
+// tiny, and a bound taken from the largest value of the loop set (a tone's)
+// would swallow their differences.
 template <int LN, bool EXACT>
-__device__ __forceinline__ int proven_median(const float (&v)[LN], int Lr, float e) {
+__device__ __forceinline__ int proven_median(const float (&v)[LN], const float (&e)[LN], int Lr) {
   float s[LN];
 #pragma unroll
   for (int j = 0; j < LN; j++) s[j] = v[j];
   const int m = (Lr - 1) >> 1;
   const float med = lower_median<LN, EXACT>(s, Lr);
   int idx = -1;
+  float em = 0.f;
 #pragma unroll
   for (int j = LN - 1; j >= 0; j--)
-    if (j < Lr && v[j] == med) idx = j;
+    if (j < Lr && v[j] == med) {
+      idx = j;
+      em = e[j];
+    }
   int below = 0, above = 0;
 #pragma unroll
   for (int j = 0; j < LN; j++) {
     if (j < Lr && j != idx) {
-      below += (v[j] < med - 2.0f * e);
-      above += (v[j] > med + 2.0f * e);
+      below += (v[j] + e[j] < med - em);
+      above += (v[j] - e[j] > med + em);
     }
   }
   return (below == m && above == Lr - 1 - m) ? idx : -1;
@@ -781,7 +788,7 @@ __device__ __forceinline__ void publish_all(const V12Dev &d, int nslots) {
 // Resident 128-thread blocks per SM the estimation kernels are compiled
 // for (registers per thread = 65536 / (128 * blocks), without spills).
 constexpr int est32_blocks(int LN) { return LN <= 18 ? 8 : LN <= 24 ? 6 : 5; }
-constexpr int est64_blocks(int LN) { return LN <= 14 ? 6 : LN <= 24 ? 5 : 4; }
+constexpr int est64_blocks(int LN) { return LN <= 14 ? 6 : LN <= 20 ? 5 : 4; }
 
 // FP32 form: values and medians in FP32.
 template <int LN, bool EXACT>
@@ -834,30 +841,32 @@ __global__ void __launch_bounds__(128, est64_blocks(LN)) k_estimate64(V12Dev d, 
     const long h = ck.base + threadIdx.x;  // one candidate per thread and chunk
     if (h < ck.end) {
       const unsigned f = cand_freq(d, ck.slot, h);
-      float re[LN], im[LN];
-      float smax = 0.f;
+      float re[LN], im[LN], eb[LN];
 #pragma unroll
       for (int j = 0; j < LN; j++) {
         if (EXACT || j < Lr) {
           float sc;
           value32(d, xs32, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
-          smax = fmaxf(smax, sc);
+          // |exact - approx| <= 2^-22 * scale: each FP32 operand carries one
+          // rounding (2^-24 relative), plus two products and a sum; the
+          // bound below has a 4x margin, which also covers the rounding of
+          // the comparisons in proven_median.
+          eb[j] = sc * 0x1p-20f + 1e-30f;
         } else {
           re[j] = INFINITY;
           im[j] = INFINITY;
+          eb[j] = 0.f;
         }
       }
-      // |exact - approx| <= 2^-20 * scale: each FP32 operand carries one
-      // rounding (2^-24 relative), plus two products and a sum; 4x margin.
-      const float e = smax * 0x1p-20f + 1e-30f;
-      const int ir = proven_median<LN, EXACT>(re, Lr, e);
-      const int ii = proven_median<LN, EXACT>(im, Lr, e);
+      const int ir = proven_median<LN, EXACT>(re, eb, Lr);
+      const int ii = proven_median<LN, EXACT>(im, eb, Lr);
       double2 res;
       if (ir >= 0 && ii >= 0) {
         res.x = value64(d, xs, ir, f, (unsigned)rp[d.L + ir]).x;
         res.y = value64(d, xs, ii, f, (unsigned)rp[d.L + ii]).y;
       } else {
         res = median64_exact(d, xs, rp, f);
+        atomicAdd(&d.counters[ck.slot * CNT_STRIDE + CNT_EXACT], 1);
       }
       const long o = (long)ck.slot * d.out_stride + h;
       d.out_idx[o] = (int)f;
@@ -1071,46 +1080,6 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
   mark(se, s);
   note_launches(3);
   return cudaSuccess;
-}
-
-// Self-test of div_rn_rcp against __ddiv_rn on pseudo-random operands
-// (splitmix64 bits: random signs, mantissas and exponents spread over
-// [2^-lo, 2^hi)); counts disagreements and fast-path hits.
-__global__ void k_div_selftest(unsigned long long seed, long count, int span, unsigned long long *out) {
-  unsigned long long bad = 0, fast = 0;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
-    auto mix = [](unsigned long long z) {
-      z += 0x9E3779B97F4A7C15ull;
-      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-      return z ^ (z >> 31);
-    };
-    const unsigned long long a = mix(seed + 2 * (unsigned long long)i), b = mix(seed + 2 * (unsigned long long)i + 1);
-    const int ea = 1023 + (int)((a >> 52) % (unsigned)(2 * span + 1)) - span;
-    const int eb = 1023 + (int)((b >> 52) % (unsigned)(2 * span + 1)) - span;
-    const double num = __longlong_as_double((long long)(((a >> 11) & 1ull) << 63 | (unsigned long long)ea << 52 |
-                                                        (a & 0xfffffffffffffull)));
-    const double den = __longlong_as_double((long long)((unsigned long long)eb << 52 | (b & 0xfffffffffffffull)));
-    const double r = __drcp_rn(den);
-    const double q = div_rn_rcp(num, den, r), ref = __ddiv_rn(num, den);
-    bad += __double_as_longlong(q) != __double_as_longlong(ref);
-    const double q0 = __dmul_rn(num, r);
-    fast += __double_as_longlong(__fma_rn(__fma_rn(-q0, den, num), r, q0)) == __double_as_longlong(q);
-  }
-  atomicAdd(&out[0], bad);
-  atomicAdd(&out[1], fast);
-}
-
-cudaError_t div_selftest(unsigned long long seed, long count, int span, unsigned long long *host_out) {
-  unsigned long long *d = nullptr;
-  cudaError_t e = cudaMalloc(&d, 2 * sizeof(unsigned long long));
-  if (e) return e;
-  cudaMemset(d, 0, 2 * sizeof(unsigned long long));
-  k_div_selftest<<<sm_count() * 8, 256>>>(seed, count, span, d);
-  e = cudaGetLastError();
-  if (!e) e = cudaMemcpy(host_out, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
-  cudaFree(d);
-  return e;
 }
 
 cudaError_t global_fft_c128(void *a, void *b, int N, int narr, long arr_stride, long slot_stride, int nslots,
