@@ -26,9 +26,10 @@ count keep the comb width (W = Comb_cst n / B_loc) fixed: a narrower comb
 lets pairs of tones share a residue class and cancel there.
 
 Run on a GPU:
-    python -m sfft_gb300.autotune --out-dir gpurun_out/tune
-writes tuned_table.inc (compiled into the library from
-sfft_gb300/csrc/tuned_table.inc) and tuned_table.json (times and errors).
+    python -m sfft_gb300.autotune --out-dir <dir>
+writes <dir>/tuned_table.inc (copy it to sfft_gb300/csrc/tuned_table.inc,
+which the library compiles in) and <dir>/tuned_table.json (times and
+errors, kept as sfft_gb300/tuned_table.json).
 """
 import argparse
 import ctypes
