@@ -816,6 +816,10 @@ void plan_draw(sfft_plan *plan, int *rp, unsigned epoch) { draw_params(*impl(pla
 
 int plan_device(sfft_plan *plan) { return impl(plan)->device; }
 
+// Device counters of the plan's batch slots (CNT_STRIDE ints per slot),
+// rewritten by every execution.
+const int *plan_counters(sfft_plan *plan) { return impl(plan)->counters.as<int>(); }
+
 void set_last_error(const char *m) { set_err(m); }
 
 // ----------------------------------------------- graph-capturable launches

@@ -19,6 +19,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <list>
@@ -32,9 +33,11 @@
 #include <vector>
 
 #include "../../include/sfft.h"
+#include "engine.h"
 
 namespace sfft {
 void set_last_error(const char *m);
+const int *plan_counters(sfft_plan *plan);
 int k_bucket(int k);
 sfft_plan *make_plan_tuned(int n, int k, int version, const sfft_options &o, int mode, bool &tuned);
 }
@@ -87,13 +90,14 @@ struct Batch {
   int *d_idx = nullptr;
   void *d_val = nullptr;
   int *d_cnt = nullptr;
+  int *d_ctr = nullptr;  // the plan's counters of this batch's slots, copied after it ran
   long bytes = 0, cap = 0;
   int collected = 0;
   size_t val_size = 16;
   std::atomic<bool> complete{false};
   // results moved to host memory to free the device (see spill_batch)
   bool spilled = false;
-  std::vector<int> h_cnt;
+  std::vector<int> h_cnt, h_err;
   std::vector<std::vector<int>> h_idx;
   std::vector<std::vector<char>> h_val;
 };
@@ -164,9 +168,11 @@ void free_batch_device(Batch *b) {
   cudaFree(b->d_idx);
   cudaFree(b->d_val);
   cudaFree(b->d_cnt);
+  cudaFree(b->d_ctr);
   b->d_idx = nullptr;
   b->d_val = nullptr;
   b->d_cnt = nullptr;
+  b->d_ctr = nullptr;
   for (size_t i = 0; i < b->reqs.size(); i++)
     if (!b->taken[i] && b->reqs[i]->staged) {
       cudaFree(b->reqs[i]->staged);
@@ -185,10 +191,14 @@ bool spill_batch(sfft_server *s, Batch *b) {
   b->h_cnt.assign(m, 0);
   b->h_idx.resize(m);
   b->h_val.resize(m);
-  if (cudaMemcpy(b->h_cnt.data(), b->d_cnt, sizeof(int) * m, cudaMemcpyDeviceToHost) != cudaSuccess) {
+  std::vector<int> ctr((size_t)m * sfft::CNT_STRIDE);
+  if (cudaMemcpy(b->h_cnt.data(), b->d_cnt, sizeof(int) * m, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(ctr.data(), b->d_ctr, sizeof(int) * ctr.size(), cudaMemcpyDeviceToHost) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
+  b->h_err.assign(m, 0);
+  for (int i = 0; i < m; i++) b->h_err[i] = ctr[(size_t)i * sfft::CNT_STRIDE + sfft::CNT_ERR];
   for (int i = 0; i < m; i++) {
     if (b->taken[i]) continue;
     const long c = std::max(0L, std::min((long)b->h_cnt[i], b->cap));
@@ -337,7 +347,7 @@ void schedule(sfft_server *s) {
     b->reqs.assign(g.second.begin(), g.second.begin() + m);
     b->taken.assign(m, 0);
     for (int i = m; i < (int)g.second.size(); i++) keep.push_back(g.second[i]);
-    const long obytes = (long)m * pe->cap * (4 + (long)b->val_size) + 4L * m;
+    const long obytes = (long)m * pe->cap * (4 + (long)b->val_size) + 4L * m + 4L * m * sfft::CNT_STRIDE;
     long sbytes = 0;
     for (Request *r : b->reqs)
       if (!r->staged && r->in_type >= 100) sbytes += (long)r->n * ((r->in_type - 100) == SFFT_IN_C64 ? 8 : 16);
@@ -357,7 +367,8 @@ void schedule(sfft_server *s) {
     cudaStream_t st = pe->stream;  // everything of this batch is ordered on the plan's stream
     bool ok = cudaMallocAsync((void **)&b->d_idx, sizeof(int) * (size_t)m * pe->cap, st) == cudaSuccess &&
               cudaMallocAsync(&b->d_val, b->val_size * (size_t)m * pe->cap, st) == cudaSuccess &&
-              cudaMallocAsync((void **)&b->d_cnt, sizeof(int) * m, st) == cudaSuccess;
+              cudaMallocAsync((void **)&b->d_cnt, sizeof(int) * m, st) == cudaSuccess &&
+              cudaMallocAsync((void **)&b->d_ctr, sizeof(int) * m * sfft::CNT_STRIDE, st) == cudaSuccess;
     std::vector<const void *> ins(m);
     std::vector<unsigned> seeds(m);
     int in_type = SFFT_IN_C128;
@@ -382,6 +393,10 @@ void schedule(sfft_server *s) {
     if (ok)
       ok = sfft_exec_batch_ex(pe->plan, m, ins.data(), in_type, seeds.data(), b->d_idx, b->d_val, b->d_cnt,
                               pe->cap, st) == 0;
+    // the slots' counters (error bits) belong to this batch once it ran
+    if (ok)
+      ok = cudaMemcpyAsync(b->d_ctr, sfft::plan_counters(pe->plan), sizeof(int) * m * sfft::CNT_STRIDE,
+                           cudaMemcpyDeviceToDevice, st) == cudaSuccess;
     if (ok) ok = cudaLaunchHostFunc(st, host_done, b) == cudaSuccess;
     if (ok) s->batches.push_back(b);
     if (!ok) {
@@ -514,12 +529,23 @@ long sfft_server_wait_for(sfft_server *s, long id, int *out_idx, complex_t *out_
   } else {
     Batch *b = r->batch;
     cudaSetDevice(s->device);
-    int cnt = 0;
+    int cnt = 0, err = 0;
     bool ok = true;
-    if (b->spilled)
+    if (b->spilled) {
       cnt = (int)b->h_idx[r->slot].size();
-    else
-      ok = cudaMemcpy(&cnt, b->d_cnt + r->slot, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+      err = b->h_err[r->slot];
+    } else {
+      ok = cudaMemcpy(&cnt, b->d_cnt + r->slot, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess &&
+           cudaMemcpy(&err, b->d_ctr + (size_t)r->slot * sfft::CNT_STRIDE + sfft::CNT_ERR, sizeof(int),
+                      cudaMemcpyDeviceToHost) == cudaSuccess;
+    }
+    if (ok && err) {  // the transform itself flagged this signal
+      char msg[160];
+      std::snprintf(msg, sizeof msg,
+                    "device reported error bits 0x%x (1 hit list, 2 output, 4 v3 no fixpoint, 8 v3 capacity)", err);
+      sfft::set_last_error(msg);
+      ok = false;
+    }
     if (ok && (out_idx || out_val) && cnt > cap) {  // no buffers: only the count is asked for
       sfft::set_last_error("output capacity too small");
       ok = false;
