@@ -230,6 +230,10 @@ long sfft_server_submit(sfft_server *s, int n, int k, enum sfft_version version,
  * values as complex128) and the submit-to-completion latency.  Returns the
  * number of coefficients, or -1. */
 long sfft_server_wait(sfft_server *s, long id, int *out_idx, complex_t *out_val, long cap, double *latency_ms);
+/* The number of coefficients of a finished request (waiting up to
+ * timeout_ms, < 0: no limit; -2 on time-out), without collecting it: size
+ * the buffers of sfft_server_wait with it. */
+long sfft_server_count(sfft_server *s, long id, double timeout_ms);
 /* As sfft_server_wait, giving up after timeout_ms (< 0: no limit): then
  * returns -2 and the request stays pending. */
 long sfft_server_wait_for(sfft_server *s, long id, int *out_idx, complex_t *out_val, long cap, double *latency_ms,

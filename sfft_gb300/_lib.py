@@ -108,6 +108,8 @@ def load(build_if_missing=False):
     L.sfft_server_submit.argtypes = [vp, ci, ci, ci, ci, vp, ci, ctypes.c_uint]
     L.sfft_server_wait.restype = cl
     L.sfft_server_wait.argtypes = [vp, cl, vp, vp, cl, ctypes.POINTER(ctypes.c_double)]
+    L.sfft_server_count.restype = cl
+    L.sfft_server_count.argtypes = [vp, cl, ctypes.c_double]
     L.sfft_server_wait_for.restype = cl
     L.sfft_server_wait_for.argtypes = L.sfft_server_wait.argtypes + [ctypes.c_double]
     L.sfft_describe_plan_params.restype = ci

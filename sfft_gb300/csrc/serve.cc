@@ -601,6 +601,39 @@ long sfft_server_wait_for(sfft_server *s, long id, int *out_idx, complex_t *out_
   return result;
 }
 
+long sfft_server_count(sfft_server *s, long id, double timeout_ms) {
+  if (!s) return -1;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) {
+    sfft::set_last_error("unknown request");
+    return -1;
+  }
+  Request *r = it->second;
+  const auto deadline = Clock::now() + std::chrono::microseconds((long)(1000.0 * std::max(0.0, timeout_ms)));
+  while (!r->done.load(std::memory_order_acquire)) {
+    if (timeout_ms >= 0 && Clock::now() >= deadline) {
+      sfft::set_last_error("timed out waiting for the request (it stays queued)");
+      return -2;
+    }
+    s->cv_done.wait_for(lk, std::chrono::microseconds(500));
+  }
+  if (r->failed) {
+    sfft::set_last_error(r->error.c_str());
+    return -1;
+  }
+  Batch *b = r->batch;
+  if (b->spilled) return (long)b->h_idx[r->slot].size();
+  cudaSetDevice(s->device);
+  int cnt = 0;
+  if (cudaMemcpy(&cnt, b->d_cnt + r->slot, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    sfft::set_last_error("count read failed");
+    return -1;
+  }
+  return cnt;
+}
+
 long sfft_server_plan_bytes(int n, int k, enum sfft_version version, int precision, int max_batch) {
   if (n < 16 || (n & (n - 1)) || k < 1 || max_batch < 1) return -1;
   const int prec = version == SFFT_VERSION_3 ? SFFT_PREC_FP64 : precision;

@@ -6,7 +6,7 @@ reference binding (python/sfft/sfft.py:33-85 of sFFT 0.1): a plan for
 Python 3 / numpy 2; the (n, k) whitelist of v1/v2 (:10-31) is a warning,
 not an error, because the library validates the domain itself; errors
 raise with the library's message; and `execute_sparse`, `precision`,
-device-array input and batched execution are added.
+`voted`, device-array input and batched execution are added.
 """
 import ctypes
 import warnings
@@ -32,7 +32,7 @@ class sfft:
     """A sparse FFT plan (python/sfft/sfft.py:33-85)."""
 
     def __init__(self, length=16384, sparsity=50, version=1, optimization=FFTW_ESTIMATE,
-                 precision="fp64", device=-1, max_batch=16):
+                 precision="fp64", device=-1, max_batch=16, voted=False):
         length = _as_int("length", length)
         sparsity = _as_int("sparsity", sparsity)
         version = _as_int("version", version)
@@ -55,6 +55,10 @@ class sfft:
                                                    ctypes.byref(opt))
         if not self.sfft_plan:
             raise RuntimeError("sfft_make_plan failed: " + _lib.last_error())
+        if voted:  # v2 only: estimate the candidates that pass the vote (not the reference's list)
+            if version != 2 or self._L.sfft_plan_v2_voted(self.sfft_plan, 1) != 0:
+                raise ValueError("the voted mode applies to version 2 plans: " + _lib.last_error())
+        self.voted = bool(voted)
         self.capacity = int(self._L.sfft_output_capacity(self.sfft_plan))
 
     # -- the reference's method ---------------------------------------------
