@@ -127,17 +127,21 @@ struct Server : sfft_server {};
 // Runs on a CUDA driver thread after the batch: no CUDA calls and no
 // server lock (plan construction may hold it); flags are atomic and the
 // waiters poll with a timeout.
+// The batch may be collected and deleted as soon as its last request is
+// marked done, so everything that touches the batch or its plan comes
+// first, and the requests are marked from a local copy of the list.
 void host_done(void *arg) {
   Batch *b = (Batch *)arg;
   sfft_server *s = (sfft_server *)b->srv;
   const auto now = Clock::now();
-  for (Request *r : b->reqs) {
+  const std::vector<Request *> reqs = b->reqs;
+  b->complete.store(true, std::memory_order_release);
+  b->pe->busy.store(false, std::memory_order_release);
+  for (Request *r : reqs) {  // a marked request may be collected at once
     r->t_done = now;
     r->done.store(true, std::memory_order_release);
   }
-  b->complete.store(true, std::memory_order_release);
-  b->pe->busy.store(false, std::memory_order_release);
-  s->cv_done.notify_all();
+  s->cv_done.notify_all();  // the server outlives its callbacks (destroy synchronises the device)
   s->cv_work.notify_all();
 }
 
