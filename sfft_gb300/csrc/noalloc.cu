@@ -20,7 +20,9 @@
 // Sharing: every call on a device uses the same array and it keeps the last
 // call's contents.  The counters and comb bitmap are cleared on the stream
 // at the start of each call; vote counters carry a per-call tag instead of
-// being cleared.  Calls whose GPU work overlaps (different streams, or
+// being cleared, and they occupy a fixed region at the start of the array
+// that nothing else is written to, so plans of different sizes can follow
+// one another.  Calls whose GPU work overlaps (different streams, or
 // different threads without ordering) race on the array.
 //
 // Set-up: the first call on each device looks up the array's device
@@ -79,8 +81,15 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
     return -1;
   }
   const size_t cs = d.prec == PREC_FP64 ? 16 : 8;
-  // layout of the static area for this plan
+  // Layout of the static area.  The vote counters come first, at a fixed
+  // offset and sized for the largest n, so that whatever plan ran before,
+  // every word of that region was written only as a vote counter
+  // ((tag << 8) | votes) or is still zero: a stale word can never pass for
+  // a counter of the current call.  The regions after it move with the
+  // plan's sizes and are rewritten before they are read.
   size_t off = 0;
+  const size_t o_score = off;
+  off += up256(sizeof(unsigned) * (size_t)SFFT_NOALLOC_MAX_N);
   const size_t o_cnt = off;
   off += up256(sizeof(int) * CNT_STRIDE);
   const size_t o_rp = off;
@@ -93,8 +102,6 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
   if (d.prec == PREC_FP64) off += up256(8 * (size_t)d.xs_size);
   const size_t o_J = off;
   off += up256(sizeof(int) * (size_t)L * d.num);
-  const size_t o_score = off;
-  off += up256(sizeof(unsigned) * (size_t)d.n);
   const size_t o_hits = off;
   off += up256(sizeof(int) * (size_t)hit_cap);
   const size_t o_bits = off;
@@ -130,9 +137,12 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
   }
   unsigned char *base = g_dev_scratch[dev];
   cudaStream_t s = (cudaStream_t)stream;
-  // a fresh vote tag per call; on wrap the vote counters are cleared
+  // A fresh vote tag per call on this device (tags start at 1; the array
+  // starts zeroed).  When the 24-bit tag would wrap, the whole counter
+  // region is cleared so that no counter of an earlier call can carry the
+  // new tag.
   if (++g_epoch[dev] >= (1u << 24)) {
-    if (cudaMemsetAsync(base + o_score, 0, sizeof(unsigned) * (size_t)d.n, s) != cudaSuccess) {
+    if (cudaMemsetAsync(base + o_score, 0, sizeof(unsigned) * (size_t)SFFT_NOALLOC_MAX_N, s) != cudaSuccess) {
       cudaGetLastError();
       set_last_error("sfft_exec_noalloc: clearing vote counters failed");
       return -1;
@@ -148,8 +158,8 @@ extern "C" long sfft_exec_noalloc(sfft_plan *plan, const void *d_in, int in_type
     set_last_error("sfft_exec_noalloc: parameter upload failed");
     return -1;
   }
-  // the vote counters of other plans' calls carry other tags: stale
-  // entries read as zero; they must cover this plan's n, which the layout ensures
+  // Counters left by earlier calls (of any plan) carry earlier tags and
+  // count as zero votes; the region holds SFFT_NOALLOC_MAX_N >= n counters.
   d.xs = base + o_xs;
   d.xs32 = d.prec == PREC_FP64 ? base + o_xs32 : nullptr;
   d.J = (int *)(base + o_J);
