@@ -5,17 +5,23 @@
 //                 contiguous Gaussian fold (:130-212) and of the permuted
 //                 Gaussian fold (:215-297), each followed by its
 //                 shared-memory FFT.  The permuted samples of the second
-//                 fold replay the reference's running phase product
-//                 (:66-87) on one thread, so their rounding matches.
-//   k_v3_peel     one CTA per signal runs alternate_fft's estimate / peel
-//                 rounds (:784-1088): bucket estimation in parallel,
-//                 subtraction of recovered tones with FP64 atomics, and the
-//                 bucket-count fixpoint test, with a bounded number of rounds.
+//                 fold use the reference's running phase product (:66-87),
+//                 replayed on one thread so its rounding matches, then
+//                 applied to the gathered samples by every thread.
+//   k_v3_peel     one thread-block cluster (8 CTAs) per signal runs
+//                 alternate_fft's estimate / peel rounds (:784-1088):
+//                 bucket estimation spread over the cluster, subtraction of
+//                 recovered tones with FP64 atomics, and the bucket-count
+//                 fixpoint test, with a bounded number of rounds.
 // The result map is a per-signal open-addressing table in global memory.
 // FP64 throughout: the phase-slope frequency decode needs phase accuracy
 // below pi/n.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "engine.h"
+
+namespace cg = cooperative_groups;
 
 namespace sfft {
 
@@ -74,19 +80,25 @@ __global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d, int role0) {
     // permute_fourier (computefourier-3.0.cc:66-87): sample i is
     // x[(ig + i*ai) mod n] * shift_i with shift_0 = e^{2 pi i ig b / n} and
     // shift_{i+1} = shift_i * e^{2 pi i ai b / n}, a running product whose
-    // rounding is part of the reference's result; one thread replays it.
+    // rounding is part of the reference's result.  The product is a serial
+    // chain of rounded complex multiplications: one thread replays it into
+    // P (no memory load on the chain), then every thread multiplies its
+    // samples by their shifts.
     double2 *P = (double2 *)d.perm + (long)slot * (d.w2 + 2) * 2 + (long)l * (d.w2 + 2);
+    const int count = chunks * N + 1;
     if (threadIdx.x == 0) {
       const double a0 = 2 * kPi * ig * bb / d.n, a1 = 2 * kPi * ai * bb / d.n;
       double2 sh = make_double2(cos(a0), sin(a0));
       const double2 st = make_double2(cos(a1), sin(a1));
-      long index = ig % d.n;
-      const int count = chunks * N + 1;
       for (int i = 0; i < count; i++) {
-        if (i >= l) P[i - l] = cmul<double>(ld_x(x, d.in_type, index), sh);
+        if (i >= l) P[i - l] = sh;
         sh = cmul<double>(sh, st);
-        index = (index + ai) % d.n;
       }
+    }
+    __syncthreads();
+    for (int i = l + threadIdx.x; i < count; i += blockDim.x) {
+      const long index = (long)(((unsigned long long)ig + (unsigned long long)i * (unsigned)ai) % (unsigned)d.n);
+      P[i - l] = cmul<double>(ld_x(x, d.in_type, index), P[i - l]);
     }
     __syncthreads();
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
@@ -240,12 +252,12 @@ __device__ void map_add(const PeelCtx &c, int key, double2 v, bool assign, int *
 }
 
 // estimate_freq_mansour_loops2 (computefourier-3.0.cc:642-776)
-__device__ void est_mansour(const PeelCtx &c, int *nfound, int cap, int *err) {
+__device__ void est_mansour(const PeelCtx &c, int *nfound, int cap, int *err, int t0, int tstride) {
   const int W = c.d->W, n = c.n;
   const double PI2 = 2 * kPi, N_OVER_PI2 = n / PI2, PI2_OVER_N = PI2 / n;
   const unsigned FREQ_MASK = ((unsigned)(n - 1) & ~((unsigned)W - 1));
   const double NORM = 1. / W, NORM2 = NORM * NORM;
-  for (int bk = threadIdx.x; bk < W; bk += blockDim.x) {
+  for (int bk = t0; bk < W; bk += tstride) {
     const double2 s0 = c.man[2 * bk], s1 = c.man[2 * bk + 1];
     const double c0 = (s0.x * s0.x + s0.y * s0.y) * NORM2;
     const double c1 = (s1.x * s1.x + s1.y * s1.y) * NORM2;
@@ -272,14 +284,14 @@ __device__ void est_mansour(const PeelCtx &c, int *nfound, int cap, int *err) {
 
 // estimate_freq_gauss_loops2 (computefourier-3.0.cc:484-640)
 __device__ void est_gauss(const PeelCtx &c, const double2 *SAMP, int B, const double2 *win,
-                          int half, int a, int b, int *nfound, int cap, int *err) {
+                          int half, int a, int b, int *nfound, int cap, int *err, int t0, int tstride) {
   const int n = c.n;
   const unsigned n1 = n - 1, B1 = B - 1;
   const double PI2 = 2 * kPi, N_OVER_PI2 = n / PI2;
   const double PI2_A_OFFSET_OVER_N = PI2 * a * c.ig / n;
   const double BUCKETS_OVER_N = (double)B / n;
   const unsigned q = n / B;
-  for (int bk = threadIdx.x; bk < B; bk += blockDim.x) {
+  for (int bk = t0; bk < B; bk += tstride) {
     const double2 s0 = SAMP[2 * bk], s1 = SAMP[2 * bk + 1];
     const double c0 = s0.x * s0.x + s0.y * s0.y;
     const double c1 = s1.x * s1.x + s1.y * s1.y;
@@ -327,9 +339,27 @@ __device__ __forceinline__ void trace_rec(const V3Dev &d, int slot, int *cnt, in
   }
 }
 
-__global__ void __launch_bounds__(1024) k_v3_peel(V3Dev d) {
-  __shared__ int s_found, s_count, s_err, s_cnt[3], s_prev[3], s_stop;
-  const int slot = blockIdx.x;
+// One thread-block cluster of V3_CLUSTER CTAs per signal runs the
+// estimate / peel rounds: every loop over buckets, estimates and map
+// entries is spread over the cluster's threads, and each block-wide
+// barrier of the round structure is a cluster barrier (release / acquire
+// at cluster scope, so the global-memory bucket arrays and the map written
+// before it are visible after it).  The round's counters live in the
+// shared memory of the cluster's first CTA and are updated through
+// distributed shared memory.  Control flow is uniform across the cluster:
+// every branch is taken on values read after a barrier.
+constexpr int V3_CLUSTER = 8;
+
+struct PeelShared {
+  int found, count, err, cnt[3], prev[3], stop;
+};
+
+__global__ void __cluster_dims__(V3_CLUSTER, 1, 1) __launch_bounds__(1024) k_v3_peel(V3Dev d) {
+  __shared__ PeelShared sh_local;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  PeelShared *S = cl.map_shared_rank(&sh_local, 0);
+  const int slot = blockIdx.x / V3_CLUSTER;
   const int *rp = d.rparams + (long)slot * d.rp_stride;
   PeelCtx c;
   c.d = &d;
@@ -352,141 +382,143 @@ __global__ void __launch_bounds__(1024) k_v3_peel(V3Dev d) {
   c.aG = wrapmul(c.a, c.ig);
   c.shift = ((wrapmul(c.ai, c.b) % d.n) + d.n) % d.n;
   int *cnt = d.counters + slot * CNT_STRIDE;
-  const int T = blockDim.x;
-  if (threadIdx.x == 0) {
-    s_found = 0;
-    s_count = 0;
-    s_err = 0;
-    s_stop = 0;
-    for (int i = 0; i < 3; i++) s_prev[i] = 0;
+  const int T = blockDim.x * V3_CLUSTER;           // the cluster's threads
+  const int gt = rank * blockDim.x + threadIdx.x;  // this thread among them
+  const bool lead = rank == 0 && threadIdx.x == 0;
+  if (lead) {
+    S->found = 0;
+    S->count = 0;
+    S->err = 0;
+    S->stop = 0;
+    for (int i = 0; i < 3; i++) S->prev[i] = 0;
   }
-  __syncthreads();
+  cl.sync();
 
   // ---- Mansour estimate; first tones are assigned, their buckets cleared
-  est_mansour(c, &s_found, d.est_cap, &s_err);
-  __syncthreads();
-  int F = min(s_found, d.est_cap);
-  for (int i = threadIdx.x; i < F; i += T) {
+  est_mansour(c, &S->found, d.est_cap, &S->err, gt, T);
+  cl.sync();
+  int F = min(S->found, d.est_cap);
+  for (int i = gt; i < F; i += T) {
     trace_rec(d, slot, cnt, -2, 0, c.est_f[i], c.est_v[i]);
-    map_add(c, c.est_f[i], c.est_v[i], true, &s_count, d.map_cap, &s_err);
+    map_add(c, c.est_f[i], c.est_v[i], true, &S->count, d.map_cap, &S->err);
     const int bk = c.est_f[i] % d.W;
     c.man[2 * bk] = make_double2(0.0, 0.0);
     c.man[2 * bk + 1] = make_double2(0.0, 0.0);
   }
-  __syncthreads();
+  cl.sync();
   if (F == d.k) {  // the reference returns before writing its output (:859-860)
-    if (threadIdx.x == 0) {
+    if (lead) {
       cnt[CNT_OUT] = 0;
       if (d.out_count) d.out_count[slot] = 0;
       cnt[CNT_V3] = -1;
     }
+    cl.sync();     // the first CTA's shared memory outlives every reader
     return;
   }
 
   // ---- first Gaussian filter: peel the known tones, estimate, peel
-  int M = min(s_count, d.map_cap);
-  for (int i = threadIdx.x; i < M; i += T) {
+  int M = min(S->count, d.map_cap);
+  for (int i = gt; i < M; i += T) {
     const int h = c.list[i];
     update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, c.tkey[h], c.tval[h], c.ig, 1,
-                 &s_err);
+                 &S->err);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) s_found = 0;
-  __syncthreads();
-  est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &s_found, d.est_cap, &s_err);
-  __syncthreads();
-  F = min(s_found, d.est_cap);
-  for (int i = threadIdx.x; i < F; i += T) {
+  if (lead) S->found = 0;
+  cl.sync();
+  est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &S->found, d.est_cap, &S->err, gt, T);
+  cl.sync();
+  F = min(S->found, d.est_cap);
+  for (int i = gt; i < F; i += T) {
     trace_rec(d, slot, cnt, -1, 1, c.est_f[i], c.est_v[i]);
-    map_add(c, c.est_f[i], c.est_v[i], false, &s_count, d.map_cap, &s_err);
+    map_add(c, c.est_f[i], c.est_v[i], false, &S->count, d.map_cap, &S->err);
     update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, c.est_f[i], c.est_v[i], c.ig, 1,
-                 &s_err);
+                 &S->err);
     update_mansour(c, c.est_f[i], c.est_v[i]);
   }
-  __syncthreads();
+  cl.sync();
 
   // ---- second (permuted) Gaussian filter: peel every known tone
-  M = min(s_count, d.map_cap);
-  for (int i = threadIdx.x; i < M; i += T) {
+  M = min(S->count, d.map_cap);
+  for (int i = gt; i < M; i += T) {
     const int h = c.list[i];
     const int key = c.tkey[h];
     const int k2 = (int)((((long long)key * c.ai) % d.n + c.shift) % d.n);
-    update_gauss(c, c.g2, (const double2 *)d.win2, d.win2_half, d.B2, k2, c.tval[h], c.aG, 1, &s_err);
+    update_gauss(c, c.g2, (const double2 *)d.win2, d.win2_half, d.B2, k2, c.tval[h], c.aG, 1, &S->err);
   }
-  __syncthreads();
+  cl.sync();
 
   // ---- round robin: G2, then Mansour, G1, G2, ... until the counts of
   //      non-empty buckets repeat after a G2 round (:959-1076)
   int stage = 2, rounds = 0;
   for (;;) {
-    if (threadIdx.x == 0) s_found = 0;
-    __syncthreads();
+    if (lead) S->found = 0;
+    cl.sync();
     if (stage == 0)
-      est_mansour(c, &s_found, d.est_cap, &s_err);
+      est_mansour(c, &S->found, d.est_cap, &S->err, gt, T);
     else if (stage == 1)
-      est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &s_found, d.est_cap, &s_err);
+      est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &S->found, d.est_cap, &S->err, gt, T);
     else
-      est_gauss(c, c.g2, d.B2, (const double2 *)d.win2, d.win2_half, c.a, c.b, &s_found, d.est_cap,
-                &s_err);
-    __syncthreads();
-    F = min(s_found, d.est_cap);
-    for (int i = threadIdx.x; i < F; i += T) {
+      est_gauss(c, c.g2, d.B2, (const double2 *)d.win2, d.win2_half, c.a, c.b, &S->found, d.est_cap, &S->err,
+                gt, T);
+    cl.sync();
+    F = min(S->found, d.est_cap);
+    for (int i = gt; i < F; i += T) {
       trace_rec(d, slot, cnt, rounds, stage, c.est_f[i], c.est_v[i]);
-      map_add(c, c.est_f[i], c.est_v[i], false, &s_count, d.map_cap, &s_err);
-      update_all(c, c.est_f[i], c.est_v[i], &s_err);
+      map_add(c, c.est_f[i], c.est_v[i], false, &S->count, d.map_cap, &S->err);
+      update_all(c, c.est_f[i], c.est_v[i], &S->err);
     }
-    __syncthreads();
+    if (stage == 2 && rounds >= 1 && lead) S->cnt[0] = S->cnt[1] = S->cnt[2] = 0;
+    cl.sync();
     if (stage == 2 && rounds >= 1) {
-      if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
-      __syncthreads();
       int cm = 0, c1 = 0, c2 = 0;
-      for (int j = threadIdx.x; j < d.B1; j += T) {
+      for (int j = gt; j < d.B1; j += T) {
         const double2 v = c.g1[j];
         c1 += (v.x * v.x + v.y * v.y > 1e-6);
       }
-      for (int j = threadIdx.x; j < d.B2; j += T) {
+      for (int j = gt; j < d.B2; j += T) {
         const double2 v = c.g2[j];
         c2 += (v.x * v.x + v.y * v.y > 1e-6);
       }
-      for (int j = threadIdx.x; j < d.W; j += T) {
+      for (int j = gt; j < d.W; j += T) {
         const double2 v = c.man[2 * j];
         const double re = v.x / d.W, im = v.y / d.W;
         cm += (re * re + im * im > 1e-6);
       }
-      atomicAdd(&s_cnt[0], cm);
-      atomicAdd(&s_cnt[1], c1);
-      atomicAdd(&s_cnt[2], c2);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        s_stop = (s_cnt[0] == s_prev[0] && s_cnt[1] == s_prev[1] && s_cnt[2] == s_prev[2]);
-        for (int i = 0; i < 3; i++) s_prev[i] = s_cnt[i];
+      if (cm) atomicAdd(&S->cnt[0], cm);
+      if (c1) atomicAdd(&S->cnt[1], c1);
+      if (c2) atomicAdd(&S->cnt[2], c2);
+      cl.sync();
+      if (lead) {
+        S->stop = (S->cnt[0] == S->prev[0] && S->cnt[1] == S->prev[1] && S->cnt[2] == S->prev[2]);
+        for (int i = 0; i < 3; i++) S->prev[i] = S->cnt[i];
       }
-      __syncthreads();
-      if (s_stop) break;
+      cl.sync();
+      if (S->stop) break;
     }
     rounds++;
     if (rounds > d.max_passes) {
-      if (threadIdx.x == 0) s_err |= ERR_V3_NOCONVERGE;
+      if (lead) atomicOr(&S->err, ERR_V3_NOCONVERGE);
       break;
     }
     stage = (stage + 1) % 3;
   }
-  __syncthreads();
+  cl.sync();
 
   // ---- output: every key of the map with its accumulated value
-  M = min(s_count, d.map_cap);
+  M = min(S->count, d.map_cap);
   const int outn = min(M, d.out_cap);
-  for (int i = threadIdx.x; i < outn; i += T) {
+  for (int i = gt; i < outn; i += T) {
     const int h = c.list[i];
     d.out_idx[(long)slot * d.out_stride + i] = c.tkey[h];
     ((double2 *)d.out_val)[(long)slot * d.out_stride + i] = c.tval[h];
   }
-  if (threadIdx.x == 0) {
+  if (lead) {
     cnt[CNT_OUT] = outn;
     if (d.out_count) d.out_count[slot] = outn;
     cnt[CNT_V3] = rounds;
-    cnt[CNT_ERR] |= s_err | (M > d.out_cap ? ERR_OUT_OVERFLOW : 0);
+    cnt[CNT_ERR] |= S->err | (M > d.out_cap ? ERR_OUT_OVERFLOW : 0);
   }
+  cl.sync();       // the first CTA's shared memory outlives every reader
 }
 
 // ---------------------------------------------------------------- launch --
@@ -530,7 +562,7 @@ cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t s, StageEvents *se) 
   }
   if ((e = cudaGetLastError())) return e;
   mark(se, s);
-  k_v3_peel<<<nslots, 1024, 0, s>>>(d);
+  k_v3_peel<<<nslots * V3_CLUSTER, 1024, 0, s>>>(d);
   mark(se, s);
   note_launches(2);
   return cudaGetLastError();
