@@ -997,24 +997,6 @@ static cudaError_t launch_estimate(const V12Dev &d, int nslots, cudaStream_t s) 
   return dispatch_estimate<k_estimate32_k>(d, nslots, sm_count(), s);
 }
 
-// v2 voting by enumeration is the default (SFFT_GB300_VOTE_ENUM=0 turns it off).
-static bool vote_enum() {
-  static const bool on = [] {
-    const char *e = getenv("SFFT_GB300_VOTE_ENUM");
-    return !e || atoi(e) != 0;
-  }();
-  return on;
-}
-
-// The split FP32 fold is the default (SFFT_GB300_FOLD_SPLIT=0 turns it off).
-static bool fold_split() {
-  static const bool on = [] {
-    const char *e = getenv("SFFT_GB300_FOLD_SPLIT");
-    return !e || atoi(e) != 0;
-  }();
-  return on;
-}
-
 template <typename R, typename In>
 static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageEvents *se) {
   cudaError_t e;
@@ -1041,7 +1023,7 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
     note_launches(1);
   }
   mark(se, s);
-  if (sizeof(R) == 4 && fold_split()) {
+  if (sizeof(R) == 4) {
     constexpr int S = 4;
     dim3 fg((unsigned)((d.xs_size * S + 255) / 256), nslots);
     k_fold_split<In, S><<<fg, 256, 0, s>>>(d);
@@ -1065,7 +1047,7 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
   }
   {
     const long cmax = std::min<long>(d.W, (long)d.comb_loops * d.num);
-    if (d.version == 1 && vote_enum() && cmax < d.q_loc) {
+    if (d.version == 1 && cmax < d.q_loc) {
       const long threads = (long)d.num * cmax * d.L_loc;
       k_vote_comb<<<dim3((unsigned)((threads + 255) / 256), nslots), 256, 0, s>>>(d, (int)cmax);
     } else {
