@@ -154,6 +154,16 @@ long sfft_exec_sparse(sfft_plan *plan, const complex_t *in, int *out_idx, comple
 int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type, int *out_idx,
                     void *out_val, int *out_count, long out_stride, void *stream);
 
+/* sfft_exec_many (src/sfft.h:167) with sparse results instead of dense
+ * n-point arrays: in[s] host or device complex128 signals; out_idx[s *
+ * out_stride + i] and out_val likewise (complex128 for FP64 plans,
+ * complex64 for FP32 v1/v2 plans), out_count[s] -- host or device buffers
+ * (page-locked host memory, e.g. from sfft_malloc, makes the copies
+ * asynchronous).  Input copies, transforms and result copies of successive
+ * chunks overlap.  Synchronous; returns 0, or -1 with sfft_last_error(). */
+int sfft_exec_many_sparse(sfft_plan *plan, int num, const complex_t *const *in, int *out_idx, void *out_val,
+                          int *out_count, long out_stride);
+
 /* As sfft_exec_batch, with the random draws of signal s taken from
  * private generators seeded with seeds[s] exactly as srandom(seeds[s]);
  * srand48(seeds[s]) would seed the reference's (seeds == NULL: the global
@@ -171,7 +181,11 @@ int sfft_sync(sfft_plan *plan);
  * precision); 4 v2 comb residues (int, count returned); 5 v3 rounds;
  * 6 v3 estimates as (round, stage, frequency, re, im) doubles;
  * 7 the 16 counters of slot 0 (0 hits, 1 comb residues, 2 outputs, 3 error
- * bits, 4 voted, 8 FP64 medians that took the all-exact path).
+ * bits, 4 voted, 8 FP64 medians that took the all-exact path); 8 / 9 the
+ * v1/v2 estimation window of the location / estimation filter as held on
+ * the device (FP64 plans: n/B entries of (c, d, c^2 + d^2, 0) doubles, the
+ * filter.freq values estimate_values divides by; FP32 plans: n/B
+ * (re, im) floats of conj(h) / |h|^2).
  * Returns the number of elements written, or -1. */
 long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap);
 

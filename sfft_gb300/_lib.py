@@ -81,6 +81,8 @@ def load(build_if_missing=False):
     L.sfft_exec_sparse.argtypes = [PP, vp, vp, vp, cl]
     L.sfft_exec_batch.restype = ci
     L.sfft_exec_batch.argtypes = [PP, ci, vp, ci, vp, vp, vp, cl, vp]
+    L.sfft_exec_many_sparse.restype = ci
+    L.sfft_exec_many_sparse.argtypes = [PP, ci, vp, vp, vp, vp, cl]
     L.sfft_sync.restype = ci
     L.sfft_sync.argtypes = [PP]
     L.sfft_debug_fetch.restype = cl

@@ -795,6 +795,72 @@ bool exec_dense_pipelined(PlanImpl &P, int num, complex_t **in, complex_t **out,
   return check_device_errors(P, num - last * chunk, (last & 1) * chunk);
 }
 
+// sfft_exec_many with sparse results: like exec_dense_pipelined, chunk c's
+// input copies (copy_in) and transform (plan stream) overlap the
+// neighbouring chunks; once chunk c-1's transform is done its counts are
+// read and exactly that many (index, value) pairs are copied out on
+// copy_out.  Values keep the plan's type (complex64 for FP32 v1/v2).
+bool exec_sparse_pipelined(PlanImpl &P, int num, const complex_t *const *in, int *out_idx, void *out_val,
+                           int *out_count, long out_stride, int chunk) {
+  const size_t nb = sizeof(double) * 2 * (size_t)P.n;
+  if (!ensure_slots(P, 2 * chunk)) return false;
+  if (!P.in_stage.ensure(nb * 2 * chunk)) return false;
+  cudaStream_t s = P.stream;
+  const size_t cs = (P.version < 2 && P.prec == sfft::PREC_FP32) ? 8 : 16;
+  const bool dev_out = is_device_ptr(out_idx);
+  const cudaMemcpyKind kind = dev_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  const int nchunks = (num + chunk - 1) / chunk;
+  std::vector<int> cnt((size_t)sfft::CNT_STRIDE * chunk);
+  // results of chunk c (slot half c & 1): wait for its transform, check it,
+  // copy its counts and pairs out
+  auto drain = [&](int c) -> bool {
+    const int half = c & 1, base = half * chunk, i0 = c * chunk, m = std::min(chunk, num - i0);
+    if (!cuda_ok(cudaEventSynchronize(P.ev_comp[half]), "sync")) return false;
+    if (!cuda_ok(cudaMemcpy(cnt.data(), P.counters.as<int>() + (size_t)base * sfft::CNT_STRIDE,
+                            sizeof(int) * sfft::CNT_STRIDE * m, cudaMemcpyDeviceToHost),
+                 "counts"))
+      return false;
+    for (int i = 0; i < m; i++) {
+      const int *ci = &cnt[(size_t)i * sfft::CNT_STRIDE];
+      if (ci[sfft::CNT_ERR]) return check_device_errors(P, m, base);
+      const long c_out = ci[sfft::CNT_OUT];
+      if (c_out > out_stride) {
+        set_err("out_stride below the result count (" + std::to_string(c_out) + ")");
+        return false;
+      }
+      out_count[i0 + i] = (int)c_out;
+      const size_t src = (size_t)(base + i) * P.out_cap, dst = (size_t)(i0 + i) * out_stride;
+      if (!cuda_ok(cudaMemcpyAsync(out_idx + dst, P.out_idx.as<int>() + src, sizeof(int) * c_out, kind, P.copy_out),
+                   "index copy") ||
+          !cuda_ok(cudaMemcpyAsync((char *)out_val + cs * dst, (char *)P.out_val.p + cs * src, cs * c_out, kind,
+                                   P.copy_out),
+                   "value copy"))
+        return false;
+    }
+    return cuda_ok(cudaEventRecord(P.ev_out[half], P.copy_out), "event");
+  };
+  for (int c = 0; c < nchunks; c++) {
+    const int half = c & 1, base = half * chunk, i0 = c * chunk, m = std::min(chunk, num - i0);
+    char *istage = (char *)P.in_stage.p + nb * base;
+    // inputs of chunk c may overwrite this half once chunk c-2's transform has read it
+    if (c >= 2 && !cuda_ok(cudaStreamWaitEvent(P.copy_in, P.ev_comp[half], 0), "wait")) return false;
+    for (int i = 0; i < m; i++)
+      if (!cuda_ok(cudaMemcpyAsync(istage + nb * i, in[i0 + i], nb, cudaMemcpyHostToDevice, P.copy_in), "input copy"))
+        return false;
+    if (!cuda_ok(cudaEventRecord(P.ev_in[half], P.copy_in), "event")) return false;
+    if (!cuda_ok(cudaStreamWaitEvent(s, P.ev_in[half], 0), "wait")) return false;
+    // this half's sparse outputs are free once chunk c-2's copies finished
+    if (c >= 2 && !cuda_ok(cudaStreamWaitEvent(s, P.ev_out[half], 0), "wait")) return false;
+    std::vector<const void *> dev_in(m);
+    for (int i = 0; i < m; i++) dev_in[i] = istage + nb * i;
+    if (!launch(P, m, dev_in.data(), sfft::IN_C128, s, nullptr, base)) return false;
+    if (!cuda_ok(cudaEventRecord(P.ev_comp[half], s), "event")) return false;
+    if (c >= 1 && !drain(c - 1)) return false;
+  }
+  if (!drain(nchunks - 1)) return false;
+  return cuda_ok(cudaStreamSynchronize(P.copy_out), "sync") && cuda_ok(cudaStreamSynchronize(s), "sync");
+}
+
 }  // namespace
 
 namespace sfft {
@@ -1244,6 +1310,21 @@ long sfft_exec_sparse(sfft_plan *plan, const complex_t *in, int *out_idx, comple
   return c;
 }
 
+int sfft_exec_many_sparse(sfft_plan *plan, int num, const complex_t *const *in, int *out_idx, void *out_val,
+                          int *out_count, long out_stride) {
+  PlanImpl *P = impl(plan);
+  if (!P || num < 0 || (num > 0 && (!in || !out_idx || !out_val || !out_count))) {
+    set_err("invalid arguments");
+    return -1;
+  }
+  if (num == 0) return 0;
+  std::lock_guard<std::mutex> g(P->mu);
+  cudaSetDevice(P->device);
+  g_err.clear();
+  const int chunk = std::max(1, std::min(P->max_batch, (num + 1) / 2));
+  return exec_sparse_pipelined(*P, num, in, out_idx, out_val, out_count, out_stride, chunk) ? 0 : -1;
+}
+
 int sfft_exec_batch(sfft_plan *plan, int num, const void *const *in, int in_type, int *out_idx, void *out_val,
                     int *out_count, long out_stride, void *stream) {
   return sfft_exec_batch_ex(plan, num, in, in_type, nullptr, out_idx, out_val, out_count, out_stride, stream);
@@ -1337,6 +1418,12 @@ long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap) {
         int cnt[sfft::CNT_STRIDE];
         if (!cuda_ok(cudaMemcpy(cnt, P->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost), "debug")) return -1;
         return fetch(P->comb_list.p, cnt[sfft::CNT_COMB], sizeof(int));
+      }
+      case 8:    // estimation window of the location filter, as uploaded:
+      case 9: {  // FP64 (c, d, c^2 + d^2, 0) doubles, FP32 conj(h)/|h|^2 floats
+        const long q = P->n / (what == 8 ? p.B_loc : p.B_est);
+        const DBuf &w = what == 8 ? P->win_a : P->win_b;
+        return P->prec == sfft::PREC_FP64 ? fetch(w.p, 4 * q, 8) : fetch(w.p, 2 * q, 4);
       }
       default:
         break;
