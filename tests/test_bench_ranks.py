@@ -18,7 +18,7 @@ ws, rank, local = bench.dist_init()
 bench.barrier(ws)
 t = bench.max_over_ranks(ws, 1.5 + rank)
 called = []
-bench.cpu_reference_throughput = lambda *a: called.append(1) or (1.0, "port", 1, [1.0])
+bench.cpu_reference_throughput = lambda *a, **kw: called.append(1) or (1.0, "port", 1, [1.0])
 class A: gpus = ws; steps = 1; warmup = 0; batch = 1; pool = 1
 bench.reference_arm(A(), ws, rank)
 print(json.dumps({"rank": rank, "ws": ws, "max": t, "reference_ran": bool(called)}))
