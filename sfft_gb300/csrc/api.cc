@@ -305,13 +305,26 @@ bool ensure_slots(PlanImpl &P, int want) {
     P.out_cap = P.version == 0 ? P.hit_cap : (int)(comb_max * (P.n / p.W_Comb));
     if (P.voted) {
       // voted v2: a candidate needs `thresh` votes; at most min(comb
-      // candidates, loc_loops * 2k * n/B / thresh) can reach it, but a signal
-      // with k tones brings about k of them plus a few collisions.  The list
-      // holds max(65536, 8 * 2k); a longer one sets ERR_HIT_OVERFLOW and the
-      // execution reports an error (nothing is dropped silently).
+      // candidates, loc_loops * 2k * n/B / thresh) can reach it.  Besides
+      // the k tones, a comb candidate that is no tone lies in one of the 2k
+      // selected buckets of a location loop with probability 2k / B, so
+      // about (comb candidates) * P[Binomial(loops, 2k / B) >= thresh] pass
+      // by chance -- a handful with the reference's constants, a large
+      // share when the constants make B small against 2k.  The list holds
+      // four times that expectation plus 8 * 2k (at least 65536); a longer
+      // one sets ERR_HIT_OVERFLOW and the execution reports an error
+      // (nothing is dropped silently).
       const long vote_max = ((long)p.loops_loc * p.B_thresh * q) / p.loops_thresh + 1;
-      P.hit_cap = (int)std::min<long>(std::min<long>((long)P.out_cap, vote_max),
-                                      std::max<long>(65536, 8L * p.B_thresh));
+      const double pv = std::min(1.0, (double)p.B_thresh / p.B_loc);
+      double tail = 0.0;
+      for (int v = p.loops_thresh; v <= p.loops_loc; v++) {
+        double c = 1.0;  // binomial coefficient C(loops_loc, v)
+        for (int t = 0; t < v; t++) c = c * (p.loops_loc - t) / (t + 1);
+        tail += c * std::pow(pv, v) * std::pow(1.0 - pv, p.loops_loc - v);
+      }
+      const double expect = tail * (double)P.out_cap;
+      const long want = std::max<long>(65536, (long)std::min(4.0 * expect, 4e9) + 8L * p.B_thresh);
+      P.hit_cap = (int)std::min<long>(std::min<long>((long)P.out_cap, vote_max), want);
       P.out_cap = P.hit_cap;
     }
     if (P.prec == sfft::PREC_FP64 && !P.xs32.ensure(8 * p.x_samp_size * S)) return false;
