@@ -189,6 +189,26 @@ namespace {
 
 int L12(const PlanImpl &P) { return P.p12.loops_loc + P.p12.loops_est; }
 
+// Bucket layout of a v1/v2 plan's x_samp (V12Dev::xs_perm): grouped by comb
+// residue for plain FP32 v2 whose comb width W is a multiple of both n / B
+// and that has at least 32 candidates per residue; natural (0) otherwise.
+// (The FP64 form keeps the natural layout: its estimation is bound by the
+// exact FP64 divisions, not by the bucket lookups.)
+int xs_perm_of(const PlanImpl &P) {
+  const auto &p = P.p12;
+  if (P.version != 1 || P.voted || P.large_b || P.prec != sfft::PREC_FP32 || p.W_Comb <= 0) return 0;
+  const long ql = P.n / p.B_loc, qe = P.n / p.B_est, R = P.n / p.W_Comb;
+  if (p.W_Comb % ql || p.W_Comb % qe || R < 32) return 0;
+  return ilog2(std::min<long>(R, 256));
+}
+
+// Position of bucket b of a loop of B buckets in the grouped layout.
+long xs_position(long b, long B, int lg) {
+  if (!lg) return b;
+  const int lt = ilog2(B) - lg;
+  return ((b & ((1L << lt) - 1)) << lg) | (b >> lt);
+}
+
 // ------------------------------------------------------------- constants --
 
 bool upload_twiddles(DBuf &b, long N, int prec) {
@@ -489,6 +509,7 @@ sfft::V12Dev v12_view(PlanImpl &P) {
   d.hit_cap = P.hit_cap;
   d.out_cap = P.out_cap;
   d.voted = P.voted;
+  d.xs_perm = xs_perm_of(P);
 
   d.out_stride = P.out_cap;
   d.rparams = P.rparams.as<int>();
@@ -679,7 +700,7 @@ bool check_device_errors(PlanImpl &P, int num, int base = 0) {
     const int e = cnt[(size_t)i * sfft::CNT_STRIDE + sfft::CNT_ERR];
     if (e) {
       char buf[160];
-      std::snprintf(buf, sizeof buf, "device reported error bits 0x%x on signal %d (1 hits, 2 output, 4 v3 no fixpoint, 8 v3 capacity)",
+      std::snprintf(buf, sizeof buf, "device reported error bits 0x%x on signal %d (1 hits, 2 output, 4 v3 no fixpoint, 8 v3 capacity, 16 copy wait timed out)",
                     e, i);
       set_err(buf);
       return false;
@@ -1425,8 +1446,22 @@ long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap) {
         for (int i = 0; i < P->n; i++) o[i] = ((raw[i] >> 8) == P->epoch[0]) ? (int)(raw[i] & 255u) : 0;
         return P->n;
       }
-      case 3:
-        return fetch(P->xs.p, p.x_samp_size, P->prec == sfft::PREC_FP64 ? 16 : 8);
+      case 3: {  // bucket values in natural order
+        const size_t es = P->prec == sfft::PREC_FP64 ? 16 : 8;
+        if (p.x_samp_size > cap) return -1;
+        std::vector<unsigned char> raw(es * p.x_samp_size);
+        if (!cuda_ok(cudaMemcpy(raw.data(), P->xs.p, raw.size(), cudaMemcpyDeviceToHost), "debug")) return -1;
+        const int lg = xs_perm_of(*P);
+        unsigned char *o = (unsigned char *)dst;
+        long base = 0;
+        for (int j = 0; j < L; j++) {
+          const long B = j < p.loops_loc ? p.B_loc : p.B_est;
+          for (long b = 0; b < B; b++)
+            std::memcpy(o + es * (base + b), raw.data() + es * (base + xs_position(b, B, lg)), es);
+          base += B;
+        }
+        return p.x_samp_size;
+      }
       case 4: {
         int cnt[sfft::CNT_STRIDE];
         if (!cuda_ok(cudaMemcpy(cnt, P->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost), "debug")) return -1;

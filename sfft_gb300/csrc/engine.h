@@ -26,7 +26,8 @@ enum Counter { CNT_HITS = 0, CNT_COMB = 1, CNT_OUT = 2, CNT_ERR = 3, CNT_VOTED =
                CNT_TRACE = 6, CNT_EST = 7, CNT_EXACT = 8, CNT_STRIDE = 16 };
 
 // Error bits reported in counters[CNT_ERR].
-enum ErrBits { ERR_HIT_OVERFLOW = 1, ERR_OUT_OVERFLOW = 2, ERR_V3_NOCONVERGE = 4, ERR_V3_CAP = 8 };
+enum ErrBits { ERR_HIT_OVERFLOW = 1, ERR_OUT_OVERFLOW = 2, ERR_V3_NOCONVERGE = 4, ERR_V3_CAP = 8,
+               ERR_WAIT_TIMEOUT = 16 };
 
 // ---------------------------------------------------------------- v1/v2 --
 struct V12Dev {
@@ -49,6 +50,12 @@ struct V12Dev {
   void *xs_tmp;             // large bucket FFTs: ping-pong partner of xs
   void *comb_buf, *comb_tmp;  // large comb FFTs: comb_loops * W per slot
   int large_buckets, large_comb;  // FFT longer than one CTA's shared memory
+  // Bucket layout of xs (and xs32).  0: natural, bucket b of a loop at b.
+  // lg > 0 (plain v2 FP32 with W a multiple of both n/B): grouped for the
+  // estimation by comb residue -- with G = 2^lg and T = B / G, bucket b of
+  // a loop sits at (b mod T) * G + b / T, so the buckets one group of G
+  // candidates of one residue reads in a loop are G consecutive entries.
+  int xs_perm;
   int *J;                   // L * num per slot
   unsigned *score;          // n per slot: (epoch << 8) | votes
   int *hits;                // hit_cap per slot

@@ -328,10 +328,14 @@ __global__ void __launch_bounds__(1024, (sizeof(R) == 4 && PER == 1) ? 2 : 1) k_
   __syncthreads();
   block_fft<R, PER>(buf, B, dlog2(B), (const c2_t<R> *)(loc ? d.tw_loc : d.tw_est));
   float2 *xs32 = d.xs32 ? (float2 *)d.xs32 + (long)slot * d.xs_size + off : nullptr;
+  // grouped layout (xs_perm): bucket i goes to (i mod T) * G + i / T
+  const int lg = d.xs_perm, lt = dlog2(B) - lg;
+  const int tmask = (1 << lt) - 1;
   for (int i = threadIdx.x; i < B; i += blockDim.x) {
     const c2_t<R> v = buf[i];
-    xs[i] = v;
-    if (xs32) xs32[i] = make_float2((float)v.x, (float)v.y);
+    const int p = lg ? ((i & tmask) << lg) | (i >> lt) : i;
+    xs[p] = v;
+    if (xs32) xs32[p] = make_float2((float)v.x, (float)v.y);
     keys[i] = pkey(cabs2<R>(v));
   }
   __syncthreads();
@@ -875,6 +879,167 @@ __global__ void __launch_bounds__(128, est64_blocks(LN)) k_estimate64(V12Dev d, 
   }
 }
 
+// ------------------------------------------- estimate by comb residue --
+//
+// Plain v2 estimates every comb candidate f = rep * W + r (r a comb residue,
+// rep < R = n / W).  When W is a multiple of q = n / B, loop j hashes f to
+//   p = f ai mod n = (r ai mod n) + W (rep ai mod R)     (mod n)
+// so the window index p mod q -- and the bucket's rounding carry -- depend
+// on r only, and the bucket is b = c0 + (W / q) (rep ai mod R) (mod B)
+// (computefourier-1.0-2.0.cc:370-378).  ai is odd, so rep -> rep ai mod R
+// is a bijection: the R candidates of a residue read R distinct buckets,
+// and a group of G = R / S of them with the same rep mod S reads the G
+// buckets congruent to one value mod T = B / G.  The bucket kernel stores
+// each loop's buckets grouped that way (xs_perm), which makes a group's
+// buckets G consecutive entries.
+//
+// One CTA estimates EC_THREADS candidates (whole groups): one thread per
+// (group, loop) computes that pair's table entry and issues one bulk
+// asynchronous copy (cp.async.bulk, completion counted in bytes on an
+// mbarrier) of the group's bucket run into shared memory; then each thread
+// reads its candidate's value of every loop from shared memory -- lanes i
+// of a warp read entries (rot + i ai) mod G, distinct mod 16, so without
+// bank conflicts -- and takes the lower medians.  Several CTAs per SM
+// overlap one CTA's copies with the others' arithmetic.  Output position
+// h = residue index * R + group * G + i; the output is a set, so its order
+// is free.
+
+constexpr int EC_THREADS = 256;            // candidates per CTA
+constexpr int EC_MAXL = 32;
+constexpr int EC_MAXU = EC_THREADS / 32;   // groups per CTA (G >= 32)
+constexpr long EC_WAIT_POLLS = 1L << 22;
+
+struct EcVal {   // one (group, loop): entry i of the group reads run[(rot + i ai) mod G]
+  int rot;
+  unsigned ai;
+  float gx, gy;  // FP32 window value conj(h) / |h|^2
+};
+
+struct EcShared {
+  EcVal v[EC_MAXU * EC_MAXL];
+  int res[EC_MAXU], grp[EC_MAXU];
+  unsigned long long bar;
+  int ok;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// mbarrier with one expected arrival (the thread that announces the bytes)
+__device__ __forceinline__ void mbar_init1(unsigned long long *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned parity) {
+  unsigned done;
+  asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+               : "=r"(done)
+               : "r"(smem_u32(bar)), "r"(parity)
+               : "memory");
+  return done != 0;
+}
+
+// at most EC_WAIT_POLLS polls (each may suspend the thread for a bounded time)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+  for (long i = 0; i < EC_WAIT_POLLS; i++)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+
+// Bulk copy global -> this CTA's shared memory, completion counted in bytes
+// on `bar` (16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+template <int LN, bool EXACT>
+__global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
+  extern __shared__ __align__(128) float2 seg[];   // [loop][EC_THREADS]
+  __shared__ EcShared sh;
+  const int slot = blockIdx.y, L = d.L, lg = d.xs_perm, G = 1 << lg, units = EC_THREADS >> lg;
+  if (blockIdx.x == 0 && threadIdx.x == 0) publish_count(d, slot, cand_total(d, slot));
+  const unsigned R = (unsigned)(d.n / d.W);
+  const long total = min((long)d.counters[slot * CNT_STRIDE + CNT_COMB] * R, (long)d.out_cap);
+  const long h0 = (long)blockIdx.x * EC_THREADS;
+  if (h0 >= total) return;
+  // total is a multiple of G: a group is wholly live or wholly past the end
+  const int live = (int)min((long)units, (total - h0) >> lg);
+  if (threadIdx.x == 0) {
+    mbar_init1(&sh.bar);
+    mbar_expect(&sh.bar, (unsigned)(live * L * G * sizeof(float2)));
+  }
+  if (threadIdx.x < units) {
+    const long h = h0 + ((long)threadIdx.x << lg);
+    const int ridx = (int)(h / R);
+    sh.res[threadIdx.x] = threadIdx.x < live ? d.comb_list[(long)slot * d.W + ridx] : -1;
+    sh.grp[threadIdx.x] = (int)((h - (long)ridx * R) >> lg);
+  }
+  __syncthreads();
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  if (threadIdx.x < live * L) {
+    const int u = threadIdx.x / L, j = threadIdx.x - u * L;
+    const Slot s = loop_slot(d, j);
+    const unsigned ai = (unsigned)rp[L + j], mask = (unsigned)d.n - 1u;
+    const unsigned p0 = ((unsigned)sh.res[u] * ai) & mask;
+    unsigned c0 = p0 >> s.lq;
+    int dist = (int)(p0 & (unsigned)(s.q - 1));
+    if (dist > (s.q >> 1)) {
+      c0++;
+      dist -= s.q;
+    }
+    const int mw = dist + ((s.q - 1) >> 1);
+    const unsigned beta = (c0 + (unsigned)(d.W / s.q) * (unsigned)sh.grp[u] * ai) & ((unsigned)s.B - 1u);
+    const int lt = dlog2((unsigned)s.B) - lg;
+    const int src = (int)s.off + (int)((beta & ((1u << lt) - 1u)) << lg);
+    const float2 g = __ldg((const float2 *)(j < d.L_loc ? d.win_loc : d.win_est) + mw);
+    sh.v[u * L + j] = EcVal{(int)(beta >> lt), ai, g.x, g.y};
+    bulk_load(seg + j * EC_THREADS + (u << lg), (const float2 *)d.xs + (long)slot * d.xs_size + src,
+              (unsigned)(G * sizeof(float2)), &sh.bar);
+  }
+  if (threadIdx.x == 0) {
+    const bool ok = mbar_wait_bounded(&sh.bar, 0);
+    if (!ok) atomicOr(&d.counters[slot * CNT_STRIDE + CNT_ERR], ERR_WAIT_TIMEOUT);
+    sh.ok = ok;
+  }
+  __syncthreads();
+  if (!sh.ok) {  // the copies still in flight land before the CTA leaves (bounded)
+    if (threadIdx.x == 0) mbar_wait_bounded(&sh.bar, 0);
+    __syncthreads();
+    return;
+  }
+  mbar_test(&sh.bar, 0);  // completed: each thread observes the copied bytes
+  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
+  if (u >= live) return;
+  const int Lr = EXACT ? LN : L;
+  const EcVal *tv = sh.v + u * L;
+  const float2 *sg = seg + (u << lg);
+  float re[LN], im[LN];
+#pragma unroll
+  for (int j = 0; j < LN; j++) {
+    if (EXACT || j < Lr) {
+      const EcVal t = tv[j];
+      const float2 x = sg[j * EC_THREADS + (int)(((unsigned)t.rot + (unsigned)i * t.ai) & (unsigned)(G - 1))];
+      re[j] = x.x * t.gx + x.y * t.gy;
+      im[j] = x.x * t.gy - x.y * t.gx;
+    } else {
+      re[j] = INFINITY;
+      im[j] = INFINITY;
+    }
+  }
+  const float mre = lower_median<LN, EXACT>(re, Lr), mim = lower_median<LN, EXACT>(im, Lr);
+  const unsigned S = R >> lg;
+  const long o = (long)slot * d.out_stride + h0 + threadIdx.x;
+  d.out_idx[o] = (int)(((unsigned)sh.grp[u] + S * (unsigned)i) * (unsigned)d.W + (unsigned)sh.res[u]);
+  ((float2 *)d.out_val)[o] = make_float2(mre, mim);
+}
+
 // ---------------------------------------------------------------- scatter --
 
 template <typename R>
@@ -991,8 +1156,25 @@ static int sm_count() {
   return cache[dev];
 }
 
+// Estimation by comb residue (xs_perm set, FP32): one CTA per EC_THREADS
+// candidates, up to min(W, comb_loops * 2k) residues of n / W candidates.
+template <int LN, bool EX>
+struct EcK32 {
+  static cudaError_t go(int nslots, cudaStream_t s, const V12Dev &d, int) {
+    const long cmax = std::min<long>(d.W, (long)d.comb_loops * d.num);
+    const long cands = std::min<long>(cmax * (d.n / d.W), (long)d.out_cap);
+    const size_t sm = sizeof(float2) * EC_THREADS * d.L;
+    cudaError_t e;
+    if ((e = set_smem(k_estimate_comb32<LN, EX>, sm))) return e;
+    dim3 g((unsigned)((cands + EC_THREADS - 1) / EC_THREADS), nslots);
+    k_estimate_comb32<LN, EX><<<g, EC_THREADS, sm, s>>>(d);
+    return cudaSuccess;
+  }
+};
+
 template <typename R>
 static cudaError_t launch_estimate(const V12Dev &d, int nslots, cudaStream_t s) {
+  if (sizeof(R) == 4 && d.xs_perm) return dispatch_estimate<EcK32>(d, nslots, 0, s);
   if (sizeof(R) == 8) return dispatch_estimate<k_estimate64_k>(d, nslots, sm_count(), s);
   return dispatch_estimate<k_estimate32_k>(d, nslots, sm_count(), s);
 }
