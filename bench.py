@@ -1013,6 +1013,29 @@ def e2e_leg(L, p32, pool, B, a):
             "error": err or None}
 
 
+def copy_bandwidth(nbytes=1 << 30, reps=5):
+    """Host<->device copy bandwidth of page-locked memory on this machine
+    (one 1 GiB cudaMemcpyAsync per direction, CUDA-event timed): the bound
+    of the host-buffer (e2e) legs."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        out[name] = reps * nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9
+    del h, d
+    torch.cuda.empty_cache()
+    return out
+
+
 def e2e_sparse_leg(L, p32, pool, B, a):
     """sfft_exec_many_sparse on page-locked host buffers: host signals in,
     host (index, value) arrays out -- the same transforms as the dense
@@ -1046,6 +1069,7 @@ def e2e_sparse_leg(L, p32, pool, B, a):
     for p in host_in + [hidx, hval]:
         L.sfft_free(p)
     return {"value": B * steps / dt, "unit": "solves/s", "h2d_bytes_per_step": B * nb, "d2h_bytes_per_step": d2h,
+            "h2d_gbs_achieved": B * nb * steps / dt / 1e9, "copy_bandwidth": copy_bandwidth(),
             "api": "sfft_exec_many_sparse, complex128 host inputs, host (int32 index, complex64 value) outputs, "
                    "pinned host"}
 

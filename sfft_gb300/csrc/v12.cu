@@ -896,7 +896,8 @@ __global__ void __launch_bounds__(128, est64_blocks(LN)) k_estimate64(V12Dev d, 
 // One CTA estimates EC_THREADS candidates (whole groups): one thread per
 // (group, loop) computes that pair's table entry and issues one bulk
 // asynchronous copy (cp.async.bulk, completion counted in bytes on an
-// mbarrier) of the group's bucket run into shared memory; then each thread
+// mbarrier that also counts the table writers' arrivals) of the group's
+// bucket run into shared memory; each thread waits on the mbarrier, then
 // reads its candidate's value of every loop from shared memory -- lanes i
 // of a warp read entries (rot + i ai) mod G, distinct mod 16, so without
 // bank conflicts -- and takes the lower medians.  Several CTAs per SM
@@ -919,15 +920,17 @@ struct EcShared {
   EcVal v[EC_MAXU * EC_MAXL];
   int res[EC_MAXU], grp[EC_MAXU];
   unsigned long long bar;
-  int ok;
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
-// mbarrier with one expected arrival (the thread that announces the bytes)
-__device__ __forceinline__ void mbar_init1(unsigned long long *bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_expect(unsigned long long *bar, unsigned bytes) {
@@ -971,23 +974,28 @@ __global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
   if (h0 >= total) return;
   // total is a multiple of G: a group is wholly live or wholly past the end
   const int live = (int)min((long)units, (total - h0) >> lg);
+  // the barrier completes once the byte count is announced, every (group,
+  // loop) thread has written its table entry and issued its copy (release),
+  // and all copied bytes have landed
   if (threadIdx.x == 0) {
-    mbar_init1(&sh.bar);
+    mbar_init(&sh.bar, 1 + live * L);
     mbar_expect(&sh.bar, (unsigned)(live * L * G * sizeof(float2)));
   }
-  if (threadIdx.x < units) {
-    const long h = h0 + ((long)threadIdx.x << lg);
-    const int ridx = (int)(h / R);
-    sh.res[threadIdx.x] = threadIdx.x < live ? d.comb_list[(long)slot * d.W + ridx] : -1;
-    sh.grp[threadIdx.x] = (int)((h - (long)ridx * R) >> lg);
-  }
   __syncthreads();
-  const int *rp = d.rparams + (long)slot * d.rp_stride;
   if (threadIdx.x < live * L) {
     const int u = threadIdx.x / L, j = threadIdx.x - u * L;
+    const long h = h0 + ((long)u << lg);
+    const int ridx = (int)(h / R);
+    const int res = d.comb_list[(long)slot * d.W + ridx];
+    const int grp = (int)((h - (long)ridx * R) >> lg);
+    if (j == 0) {
+      sh.res[u] = res;
+      sh.grp[u] = grp;
+    }
+    const int *rp = d.rparams + (long)slot * d.rp_stride;
     const Slot s = loop_slot(d, j);
     const unsigned ai = (unsigned)rp[L + j], mask = (unsigned)d.n - 1u;
-    const unsigned p0 = ((unsigned)sh.res[u] * ai) & mask;
+    const unsigned p0 = ((unsigned)res * ai) & mask;
     unsigned c0 = p0 >> s.lq;
     int dist = (int)(p0 & (unsigned)(s.q - 1));
     if (dist > (s.q >> 1)) {
@@ -995,27 +1003,22 @@ __global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
       dist -= s.q;
     }
     const int mw = dist + ((s.q - 1) >> 1);
-    const unsigned beta = (c0 + (unsigned)(d.W / s.q) * (unsigned)sh.grp[u] * ai) & ((unsigned)s.B - 1u);
+    const unsigned beta = (c0 + (unsigned)(d.W / s.q) * (unsigned)grp * ai) & ((unsigned)s.B - 1u);
     const int lt = dlog2((unsigned)s.B) - lg;
     const int src = (int)s.off + (int)((beta & ((1u << lt) - 1u)) << lg);
     const float2 g = __ldg((const float2 *)(j < d.L_loc ? d.win_loc : d.win_est) + mw);
     sh.v[u * L + j] = EcVal{(int)(beta >> lt), ai, g.x, g.y};
     bulk_load(seg + j * EC_THREADS + (u << lg), (const float2 *)d.xs + (long)slot * d.xs_size + src,
               (unsigned)(G * sizeof(float2)), &sh.bar);
+    mbar_arrive(&sh.bar);
   }
-  if (threadIdx.x == 0) {
-    const bool ok = mbar_wait_bounded(&sh.bar, 0);
-    if (!ok) atomicOr(&d.counters[slot * CNT_STRIDE + CNT_ERR], ERR_WAIT_TIMEOUT);
-    sh.ok = ok;
-  }
-  __syncthreads();
-  if (!sh.ok) {  // the copies still in flight land before the CTA leaves (bounded)
-    if (threadIdx.x == 0) mbar_wait_bounded(&sh.bar, 0);
-    __syncthreads();
+  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
+  // every thread waits (bounded) on its own; no barrier of the CTA follows
+  if (!mbar_wait_bounded(&sh.bar, 0)) {
+    atomicOr(&d.counters[slot * CNT_STRIDE + CNT_ERR], ERR_WAIT_TIMEOUT);
+    mbar_wait_bounded(&sh.bar, 0);  // copies still in flight land before the CTA leaves
     return;
   }
-  mbar_test(&sh.bar, 0);  // completed: each thread observes the copied bytes
-  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
   if (u >= live) return;
   const int Lr = EXACT ? LN : L;
   const EcVal *tv = sh.v + u * L;
@@ -1092,8 +1095,14 @@ static cudaError_t launch_comb(const V12Dev &d, int nslots, cudaStream_t s) {
 template <typename R>
 static cudaError_t launch_bucket(const V12Dev &d, int nslots, cudaStream_t s) {
   const int Bmax = d.B_loc > d.B_est ? d.B_loc : d.B_est;
-  int T, per;
-  fft_shape(Bmax, T, per);
+  // FP64: two butterflies per thread and stage -- half-size CTAs, two per SM,
+  // so one CTA's stage barriers overlap the other's FP64 arithmetic
+  // (measured 0.52 -> 0.455 ms per 32 signals at n = 2^22, k = 100; the FP32
+  // form is faster with one butterfly per thread)
+  int T = sizeof(R) == 8 ? Bmax / 8 : Bmax / 4, per;
+  if (T > 1024) T = 1024;
+  if (T < 32) T = 32;
+  per = (Bmax / 4 + T - 1) / T;
   const size_t sm = BucketSmem<R>::bytes(Bmax, d.num);
   dim3 grid(d.L, nslots);
   cudaError_t e;
