@@ -275,6 +275,8 @@ sfft_mixed *sfft_mixed_create(int num, const int *n, const int *k, const int *ve
 /* One execution: in[i] device pointers; seeds (or NULL) as in
  * sfft_exec_batch_ex.  Asynchronous; sfft_mixed_sync waits. */
 int sfft_mixed_exec(sfft_mixed *m, const void *const *in, const unsigned *seeds);
+/* Waits for the last execution; -1 (message in sfft_last_error()) if a
+ * kernel flagged one of its signals. */
 int sfft_mixed_sync(sfft_mixed *m);
 /* Device pointers to signal s's result (indices, values of value_bytes =
  * 16 (complex128) or 8 (complex64) each, capacity); returns its count. */
@@ -283,6 +285,13 @@ int sfft_mixed_result(sfft_mixed *m, int s, const int **idx, const void **val, i
  * Returns the signal's count, or -1. */
 long sfft_mixed_result_host(sfft_mixed *m, int s, int *idx, void *val, long cap);
 int sfft_mixed_groups(const sfft_mixed *m);
+/* Before the first sfft_mixed_exec: run every plain FP32 v2 group whose
+ * FFTs fit in shared memory with one persistent kernel instead of one
+ * branch of kernels per group -- a device work queue of (stage, plan,
+ * signal, tile) items in dependency order with per-signal completion
+ * counters and bounded waits.  Other groups keep their branches in the same
+ * graph.  Returns 0, or -1 with sfft_last_error(). */
+int sfft_mixed_set_persistent(sfft_mixed *m, int on);
 /* The stream (cudaStream_t) the batch's graph runs on. */
 void *sfft_mixed_stream(const sfft_mixed *m);
 void sfft_mixed_destroy(sfft_mixed *m);

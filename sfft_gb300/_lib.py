@@ -133,6 +133,8 @@ def load(build_if_missing=False):
                                     ctypes.POINTER(cl)]
     L.sfft_mixed_result_host.restype = cl
     L.sfft_mixed_result_host.argtypes = [vp, ci, vp, vp, cl]
+    L.sfft_mixed_set_persistent.restype = ci
+    L.sfft_mixed_set_persistent.argtypes = [vp, ci]
     L.sfft_mixed_groups.restype = ci
     L.sfft_mixed_groups.argtypes = [vp]
     L.sfft_mixed_destroy.argtypes = [vp]

@@ -968,6 +968,40 @@ bool plan_stage(sfft_plan *plan, int num, const void *const *in, const unsigned 
   return true;
 }
 
+// The view of a staged v1/v2 launch of `num` signals writing into the given
+// outputs, for the persistent executor (no launch).
+bool plan_staged_view(sfft_plan *plan, int num, int in_type, int *out_idx, void *out_val, int *out_count, long stride,
+                      V12Dev *d) {
+  PlanImpl *P = impl(plan);
+  if (!P || P->version > 1 || num > P->staged_slots) return false;
+  std::lock_guard<std::mutex> g(P->mu);
+  *d = v12_view(*P);
+  d->in_type = in_type;
+  d->out_idx = out_idx;
+  d->out_val = out_val;
+  d->out_count = out_count;
+  d->out_stride = stride;
+  return true;
+}
+
+// Per call of the persistent executor, capturable: the staged draws and
+// input pointers go to the device, the counters and comb bitmaps of `num`
+// slots are cleared (what v12_run does before its first kernel).
+bool plan_persist_prepare(sfft_plan *plan, int num, cudaStream_t s) {
+  PlanImpl *P = impl(plan);
+  if (!P || P->version > 1 || num > P->staged_slots) return false;
+  std::lock_guard<std::mutex> g(P->mu);
+  const auto &p = P->p12;
+  return cuda_ok(cudaMemcpyAsync(P->rparams.p, P->h_rp, sizeof(int) * (size_t)P->rp_stride * num,
+                                 cudaMemcpyHostToDevice, s),
+                 "params upload") &&
+         cuda_ok(cudaMemcpyAsync(P->inputs.p, P->h_in, sizeof(void *) * num, cudaMemcpyHostToDevice, s),
+                 "pointer upload") &&
+         cuda_ok(cudaMemsetAsync(P->counters.p, 0, sizeof(int) * sfft::CNT_STRIDE * num, s), "memset") &&
+         cuda_ok(cudaMemsetAsync(P->comb_bits.p, 0, sizeof(unsigned) * ((p.W_Comb + 31) / 32) * (size_t)num, s),
+                 "memset");
+}
+
 // Device side of a staged launch, capturable into a CUDA graph: copies the
 // staging, then the batched pipeline writing into the given outputs.
 bool plan_launch_staged(sfft_plan *plan, int num, int in_type, int *out_idx, void *out_val, int *out_count,

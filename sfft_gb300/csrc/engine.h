@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace sfft {
@@ -84,6 +85,46 @@ cudaError_t scatter_dense(const int *out_idx, const void *out_val, int prec, con
 
 // Maximum bucket-FFT length held in one CTA's shared memory.
 int v12_max_fft(int prec);
+
+// ------------------------------------------- persistent uneven executor --
+// One persistent kernel runs the whole v2 pipeline of several FP32 plans
+// (plain v2, FFTs in shared memory): a device work queue of (stage, plan,
+// signal, tile) items in dependency order, per-signal completion counters
+// in global memory, bounded waits.
+enum PersistKind { PK_COMB = 0, PK_FOLD = 1, PK_LIST = 2, PK_BUCKET = 3, PK_VOTE = 4, PK_EST = 5 };
+struct PersistGroup {
+  V12Dev d;          // the plan's view: staged draws and inputs, outputs in the caller's arena
+  int gslot0;        // first global signal slot of this plan
+  int slots;         // its signals
+  int per_comb, per_bucket;   // butterflies per thread of the comb / bucket FFTs (1, 2, 4)
+  int fold_chunks;   // 1024-thread chunks of the fold per item
+  int vote_cmax, vote_chunks; // k_vote_comb's residue bound, 1024-thread chunks per item
+  int est_comb;      // 1: estimation by comb residue (1024 candidates per item), 0: random lookups
+  int est_chunks;    // random lookups: 1024-candidate chunks per item
+  int nfold, nvote, nest;     // items per signal of those stages
+  int pad;
+};
+struct PersistItem {
+  int kind, group, slot, idx;
+};
+struct PersistProg {
+  const PersistGroup *groups;  // device
+  const PersistItem *items;    // device, dependency order
+  int nitems;
+  int *state;                  // device: queue head, abort flag, 4 counters per global slot (zeroed per run)
+  int nslots_total;
+  size_t smem;                 // dynamic shared memory per CTA
+  int in_type;
+};
+// Dependency-ordered item list for `groups` (host copies; d must be set).
+void persist_items(const PersistGroup *groups, int ngroups, std::vector<PersistItem> &items);
+// Shared memory the executor needs for these groups, and whether a plan
+// view qualifies (plain FP32 v2, FFTs in shared memory, at most 32 loops).
+size_t persist_smem(const PersistGroup *groups, int ngroups);
+bool persist_eligible(const V12Dev &d);
+// Fills a group's launch shape from its view.
+void persist_shape(PersistGroup &g);
+cudaError_t persist_run(const PersistProg &p, cudaStream_t s);
 
 // -------------------------------------------------------------------- v3 --
 struct V3Dev {

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <map>
 #include <mutex>
 #include <string>
@@ -21,8 +22,14 @@
 
 #include "../../include/sfft.h"
 
+#include "engine.h"
+
 namespace sfft {
 void set_last_error(const char *m);
+bool plan_staged_view(sfft_plan *plan, int num, int in_type, int *out_idx, void *out_val, int *out_count, long stride,
+                      V12Dev *d);
+bool plan_persist_prepare(sfft_plan *plan, int num, cudaStream_t s);
+const int *plan_counters(sfft_plan *plan);
 bool plan_enable_staging(sfft_plan *plan, int slots);
 bool plan_stage(sfft_plan *plan, int num, const void *const *in, const unsigned *seeds);
 bool plan_launch_staged(sfft_plan *plan, int num, int in_type, int *out_idx, void *out_val, int *out_count,
@@ -41,6 +48,7 @@ struct Group {
   long cap = 0, idx_off = 0, cnt_off = 0;
   size_t vsize = 16, val_off = 0;
   bool tuned = false;
+  bool persist = false;  // run by the persistent executor
 };
 }  // namespace
 
@@ -54,6 +62,13 @@ struct sfft_mixed {
   cudaEvent_t fork = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // persistent executor (sfft_mixed_set_persistent)
+  bool persistent = false;
+  sfft::PersistProg prog{};
+  sfft::PersistGroup *d_groups = nullptr;
+  sfft::PersistItem *d_items = nullptr;
+  int *d_state = nullptr;
+  int persist_groups = 0;
   std::mutex mu;
 };
 
@@ -82,10 +97,21 @@ bool stage_all(sfft_mixed *m, const void *const *in, const unsigned *seeds) {
   return true;
 }
 
-// Forks every group from `master` onto its plan's stream and joins back.
+// Forks every group the persistent executor does not run from `master` onto
+// its plan's stream and joins back; the executor's groups run as one kernel
+// on `master`.
 bool launch_all(sfft_mixed *m) {
   if (!ok(cudaEventRecord(m->fork, m->master), "fork")) return false;
+  if (m->persistent && m->persist_groups) {
+    for (Group &g : m->groups)
+      if (g.persist && !sfft::plan_persist_prepare(g.plan, (int)g.members.size(), m->master)) {
+        sfft::set_last_error("persistent executor: staging upload failed");
+        return false;
+      }
+    if (!ok(sfft::persist_run(m->prog, m->master), "persistent executor")) return false;
+  }
   for (Group &g : m->groups) {
+    if (g.persist) continue;
     if (!ok(cudaStreamWaitEvent(g.stream, m->fork, 0), "fork wait")) return false;
     if (!sfft::plan_launch_staged(g.plan, (int)g.members.size(), m->in_type, m->d_idx + g.idx_off,
                                   m->d_val + g.val_off, m->d_cnt + g.cnt_off, g.cap, g.stream))
@@ -191,7 +217,11 @@ int sfft_mixed_exec(sfft_mixed *m, const void *const *in, const unsigned *seeds)
   // first call: run directly (its results are this call's), then capture
   if (!launch_all(m) || !ok(cudaStreamSynchronize(m->master), "sync")) return -1;
   if (!ok(cudaStreamBeginCapture(m->master, cudaStreamCaptureModeThreadLocal), "capture")) return -1;
+  const long counted = sfft_kernel_launches();
   const bool launched = launch_all(m);
+  // captured launches run when the graph is replayed; this call launched
+  // only the direct ones
+  sfft::note_launches(counted - sfft_kernel_launches());
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(m->master, &g);
   if (!launched || !ok(e, "end capture")) {
@@ -206,7 +236,84 @@ int sfft_mixed_exec(sfft_mixed *m, const void *const *in, const unsigned *seeds)
 int sfft_mixed_sync(sfft_mixed *m) {
   if (!m) return -1;
   std::lock_guard<std::mutex> lk(m->mu);
-  return ok(cudaStreamSynchronize(m->master), "sync") ? 0 : -1;
+  if (!ok(cudaStreamSynchronize(m->master), "sync")) return -1;
+  // error bits the kernels set for any signal (hit-list overflow, a wait
+  // of the persistent executor that ran out, ...)
+  for (const Group &g : m->groups) {
+    const int cnt = (int)g.members.size();
+    std::vector<int> c((size_t)sfft::CNT_STRIDE * cnt);
+    if (!ok(cudaMemcpy(c.data(), sfft::plan_counters(g.plan), sizeof(int) * c.size(), cudaMemcpyDeviceToHost),
+            "counters"))
+      return -1;
+    for (int i = 0; i < cnt; i++) {
+      const int e = c[(size_t)i * sfft::CNT_STRIDE + sfft::CNT_ERR];
+      if (e) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "device reported error bits 0x%x on signal %d", e, g.members[i]);
+        sfft::set_last_error(buf);
+        return -1;
+      }
+    }
+  }
+  return 0;
+}
+
+int sfft_mixed_set_persistent(sfft_mixed *m, int on) {
+  if (!m) {
+    sfft::set_last_error("invalid arguments");
+    return -1;
+  }
+  std::lock_guard<std::mutex> lk(m->mu);
+  if (m->exec || m->persistent) {
+    sfft::set_last_error("the persistent executor is chosen before the first execution");
+    return -1;
+  }
+  if (!on) return 0;
+  cudaSetDevice(m->device);
+  std::vector<sfft::PersistGroup> pg;
+  int slots = 0;
+  for (Group &g : m->groups) {
+    sfft::PersistGroup p{};
+    const int cnt = (int)g.members.size();
+    if (!sfft::plan_staged_view(g.plan, cnt, m->in_type, m->d_idx + g.idx_off, m->d_val + g.val_off,
+                                m->d_cnt + g.cnt_off, g.cap, &p.d) ||
+        !sfft::persist_eligible(p.d))
+      continue;
+    p.gslot0 = slots;
+    p.slots = cnt;
+    sfft::persist_shape(p);
+    slots += cnt;
+    g.persist = true;
+    pg.push_back(p);
+  }
+  std::vector<sfft::PersistItem> items;
+  sfft::persist_items(pg.data(), (int)pg.size(), items);
+  const size_t smem = sfft::persist_smem(pg.data(), (int)pg.size());
+  if (smem > 200 * 1024) {  // with the executor's static shared memory, above a CTA's 227 KB
+    for (Group &g : m->groups) g.persist = false;
+    sfft::set_last_error("persistent executor: a plan needs more shared memory than one CTA has");
+    return -1;
+  }
+  if (!pg.empty() &&
+      (!ok(cudaMalloc((void **)&m->d_groups, sizeof(sfft::PersistGroup) * pg.size()), "executor") ||
+       !ok(cudaMalloc((void **)&m->d_items, sizeof(sfft::PersistItem) * std::max<size_t>(1, items.size())),
+           "executor") ||
+       !ok(cudaMalloc((void **)&m->d_state, sizeof(int) * (2 + 4 * (size_t)slots)), "executor") ||
+       !ok(cudaMemcpy(m->d_groups, pg.data(), sizeof(sfft::PersistGroup) * pg.size(), cudaMemcpyHostToDevice),
+           "executor") ||
+       !ok(cudaMemcpy(m->d_items, items.data(), sizeof(sfft::PersistItem) * items.size(), cudaMemcpyHostToDevice),
+           "executor")))
+    return -1;
+  m->prog.groups = m->d_groups;
+  m->prog.items = m->d_items;
+  m->prog.nitems = (int)items.size();
+  m->prog.state = m->d_state;
+  m->prog.nslots_total = slots;
+  m->prog.smem = smem;
+  m->prog.in_type = m->in_type;
+  m->persist_groups = (int)pg.size();
+  m->persistent = true;
+  return 0;
 }
 
 int sfft_mixed_result(sfft_mixed *m, int s, const int **idx, const void **val, int *value_bytes, long *cap) {
@@ -259,6 +366,9 @@ void sfft_mixed_destroy(sfft_mixed *m) {
   cudaFree(m->d_idx);
   cudaFree(m->d_val);
   cudaFree(m->d_cnt);
+  cudaFree(m->d_groups);
+  cudaFree(m->d_items);
+  cudaFree(m->d_state);
   delete m;
 }
 

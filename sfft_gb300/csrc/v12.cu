@@ -99,9 +99,7 @@ __global__ void __launch_bounds__(256) k_fold(V12Dev d) {
 // from DRAM repeatedly.  The summation order differs from the reference's,
 // which the FP32 form does not reproduce anyway.
 template <typename In, int S>
-__global__ void __launch_bounds__(256) k_fold_split(V12Dev d) {
-  const int slot = blockIdx.y;
-  const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void fold_split_thread(const V12Dev &d, int slot, long gt) {
   const long g = gt / S;
   const int part = (int)(gt % S);
   const bool live = g < d.xs_size;
@@ -153,6 +151,11 @@ __global__ void __launch_bounds__(256) k_fold_split(V12Dev d) {
   if (live && part == 0) ((float2 *)d.xs)[(long)slot * d.xs_size + g] = acc;
 }
 
+template <typename In, int S>
+__global__ void __launch_bounds__(256) k_fold_split(V12Dev d) {
+  fold_split_thread<In, S>(d, blockIdx.y, (long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ---------------------------------------------------------- smem layout --
 
 template <typename R>
@@ -175,9 +178,8 @@ __device__ __forceinline__ void carve(unsigned char *smem, int B, c2_t<R> *&buf,
 // ------------------------------------------------------------------ comb --
 
 template <typename R, int PER, typename In>
-__global__ void __launch_bounds__(1024) k_comb(V12Dev d) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int c = blockIdx.x, slot = blockIdx.y, W = d.W;
+__device__ __forceinline__ void comb_block(const V12Dev &d, int c, int slot, unsigned char *smem) {
+  const int W = d.W;
   c2_t<R> *buf;
   key_t<R> *keys;
   int *hist, *scan, *Js;
@@ -196,9 +198,15 @@ __global__ void __launch_bounds__(1024) k_comb(V12Dev d) {
   for (int i = threadIdx.x; i < d.num; i += blockDim.x) atomicOr(&bits[Js[i] >> 5], 1u << (Js[i] & 31));
 }
 
-__global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) {
+template <typename R, int PER, typename In>
+__global__ void __launch_bounds__(1024) k_comb(V12Dev d) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  comb_block<R, PER, In>(d, blockIdx.x, blockIdx.y, smem);
+}
+
+__device__ __forceinline__ void comb_list_block(const V12Dev &d, int slot) {
   __shared__ int scan[64];
-  const int slot = blockIdx.x, W = d.W;
+  const int W = d.W;
   const int words = (W + 31) >> 5;
   const unsigned *bits = d.comb_bits + (long)slot * words;
   const int C = (words + blockDim.x - 1) / blockDim.x;
@@ -218,6 +226,8 @@ __global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) {
   }
   if (threadIdx.x == 0) d.counters[slot * CNT_STRIDE + CNT_COMB] = tot.x;
 }
+
+__global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) { comb_list_block(d, blockIdx.x); }
 
 // Voting of the location loops, one thread per (loop, selected bucket,
 // position): positions p in [J*q - floor(q/2), +q) (mod n)
@@ -284,10 +294,8 @@ __global__ void __launch_bounds__(256) k_vote(V12Dev d) {
 // mod W are p = c (mod W) with c = r a^-1 mod W (a odd; W divides n) -- one
 // thread per (loop, bucket, residue) visits exactly those, instead of one
 // thread per position testing the residue bitmap.  Same votes, any order.
-__global__ void __launch_bounds__(256) k_vote_comb(V12Dev d, int cmax) {
-  const int slot = blockIdx.y;
+__device__ __forceinline__ void vote_comb_thread(const V12Dev &d, int cmax, int slot, long g) {
   const long per_loop = (long)d.num * cmax;
-  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= per_loop * d.L_loc) return;
   const int j = (int)(g / per_loop);
   const long e = g - (long)j * per_loop;
@@ -310,12 +318,14 @@ __global__ void __launch_bounds__(256) k_vote_comb(V12Dev d, int cmax) {
   }
 }
 
+__global__ void __launch_bounds__(256) k_vote_comb(V12Dev d, int cmax) {
+  vote_comb_thread(d, cmax, blockIdx.y, (long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ---------------------------------------------------------------- bucket --
 
 template <typename R, int PER>
-__global__ void __launch_bounds__(1024, (sizeof(R) == 4 && PER == 1) ? 2 : 1) k_bucket(V12Dev d) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int j = blockIdx.x, slot = blockIdx.y;
+__device__ __forceinline__ void bucket_block(const V12Dev &d, int j, int slot, unsigned char *smem) {
   const bool loc = j < d.L_loc;
   const int B = loc ? d.B_loc : d.B_est;
   const long off = loc ? (long)j * d.B_loc : (long)d.L_loc * d.B_loc + (long)(j - d.L_loc) * d.B_est;
@@ -342,6 +352,12 @@ __global__ void __launch_bounds__(1024, (sizeof(R) == 4 && PER == 1) ? 2 : 1) k_
   block_top_indices<key_t<R>>(keys, B, d.num, Js, hist, scan);
   int *Jg = d.J + ((long)slot * d.L + j) * d.num;
   for (int i = threadIdx.x; i < d.num; i += blockDim.x) Jg[i] = Js[i];
+}
+
+template <typename R, int PER>
+__global__ void __launch_bounds__(1024, (sizeof(R) == 4 && PER == 1) ? 2 : 1) k_bucket(V12Dev d) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  bucket_block<R, PER>(d, blockIdx.x, blockIdx.y, smem);
 }
 
 // ------------------------------------------------- FFTs beyond one CTA --
@@ -794,6 +810,31 @@ __device__ __forceinline__ void publish_all(const V12Dev &d, int nslots) {
 constexpr int est32_blocks(int LN) { return LN <= 18 ? 8 : LN <= 24 ? 6 : 5; }
 constexpr int est64_blocks(int LN) { return LN <= 14 ? 6 : LN <= 20 ? 5 : 4; }
 
+// One FP32 candidate h (< the slot's total) by random bucket lookups.
+template <int LN, bool EXACT>
+__device__ __forceinline__ void est32_candidate(const V12Dev &d, int slot, long h) {
+  const float2 *wl = (const float2 *)d.win_loc, *we = (const float2 *)d.win_est;
+  const int Lr = EXACT ? LN : d.L;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const float2 *xs = (const float2 *)d.xs + (long)slot * d.xs_size;
+  const unsigned f = cand_freq(d, slot, h);
+  float re[LN], im[LN];
+#pragma unroll
+  for (int j = 0; j < LN; j++) {
+    if (EXACT || j < Lr) {
+      float sc;
+      value32(d, xs, wl, we, j, f, (unsigned)rp[d.L + j], re[j], im[j], sc);
+    } else {
+      re[j] = INFINITY;
+      im[j] = INFINITY;
+    }
+  }
+  const float mre = lower_median<LN, EXACT>(re, Lr), mim = lower_median<LN, EXACT>(im, Lr);
+  const long o = (long)slot * d.out_stride + h;
+  d.out_idx[o] = (int)f;
+  ((float2 *)d.out_val)[o] = make_float2(mre, mim);
+}
+
 // FP32 form: values and medians in FP32.
 template <int LN, bool EXACT>
 __global__ void __launch_bounds__(128, est32_blocks(LN)) k_estimate32(V12Dev d, int nslots) {
@@ -905,9 +946,8 @@ __global__ void __launch_bounds__(128, est64_blocks(LN)) k_estimate64(V12Dev d, 
 // h = residue index * R + group * G + i; the output is a set, so its order
 // is free.
 
-constexpr int EC_THREADS = 256;            // candidates per CTA
+constexpr int EC_THREADS = 256;            // candidates per CTA of k_estimate_comb32
 constexpr int EC_MAXL = 32;
-constexpr int EC_MAXU = EC_THREADS / 32;   // groups per CTA (G >= 32)
 constexpr long EC_WAIT_POLLS = 1L << 22;
 
 struct EcVal {   // one (group, loop): entry i of the group reads run[(rot + i ai) mod G]
@@ -916,9 +956,11 @@ struct EcVal {   // one (group, loop): entry i of the group reads run[(rot + i a
   float gx, gy;  // FP32 window value conj(h) / |h|^2
 };
 
+// Shared state of one item of NTH candidates (groups of G >= 32).
+template <int NTH>
 struct EcShared {
-  EcVal v[EC_MAXU * EC_MAXL];
-  int res[EC_MAXU], grp[EC_MAXU];
+  EcVal v[(NTH / 32) * EC_MAXL];
+  int res[NTH / 32], grp[NTH / 32];
   unsigned long long bar;
 };
 
@@ -962,17 +1004,17 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
                : "memory");
 }
 
-template <int LN, bool EXACT>
-__global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
-  extern __shared__ __align__(128) float2 seg[];   // [loop][EC_THREADS]
-  __shared__ EcShared sh;
-  const int slot = blockIdx.y, L = d.L, lg = d.xs_perm, G = 1 << lg, units = EC_THREADS >> lg;
-  if (blockIdx.x == 0 && threadIdx.x == 0) publish_count(d, slot, cand_total(d, slot));
+// Candidates [h0, h0 + NTH) of a slot (h0 < total, the slot's candidate
+// count; total is a multiple of G, so a group is wholly live or wholly past
+// the end).  Every thread of a block of NTH threads calls it; seg holds
+// L * NTH float2.  The mbarrier in sh is initialised here; a caller that
+// runs another item with the same sh invalidates it first, after a block
+// barrier.
+template <int LN, bool EXACT, int NTH>
+__device__ __forceinline__ void ec32_block(const V12Dev &d, int slot, long h0, long total, float2 *seg,
+                                           EcShared<NTH> &sh) {
+  const int L = d.L, lg = d.xs_perm, G = 1 << lg, units = NTH >> lg;
   const unsigned R = (unsigned)(d.n / d.W);
-  const long total = min((long)d.counters[slot * CNT_STRIDE + CNT_COMB] * R, (long)d.out_cap);
-  const long h0 = (long)blockIdx.x * EC_THREADS;
-  if (h0 >= total) return;
-  // total is a multiple of G: a group is wholly live or wholly past the end
   const int live = (int)min((long)units, (total - h0) >> lg);
   // the barrier completes once the byte count is announced, every (group,
   // loop) thread has written its table entry and issued its copy (release),
@@ -1008,15 +1050,15 @@ __global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
     const int src = (int)s.off + (int)((beta & ((1u << lt) - 1u)) << lg);
     const float2 g = __ldg((const float2 *)(j < d.L_loc ? d.win_loc : d.win_est) + mw);
     sh.v[u * L + j] = EcVal{(int)(beta >> lt), ai, g.x, g.y};
-    bulk_load(seg + j * EC_THREADS + (u << lg), (const float2 *)d.xs + (long)slot * d.xs_size + src,
+    bulk_load(seg + j * NTH + (u << lg), (const float2 *)d.xs + (long)slot * d.xs_size + src,
               (unsigned)(G * sizeof(float2)), &sh.bar);
     mbar_arrive(&sh.bar);
   }
   const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
-  // every thread waits (bounded) on its own; no barrier of the CTA follows
+  // every thread waits (bounded) on its own
   if (!mbar_wait_bounded(&sh.bar, 0)) {
     atomicOr(&d.counters[slot * CNT_STRIDE + CNT_ERR], ERR_WAIT_TIMEOUT);
-    mbar_wait_bounded(&sh.bar, 0);  // copies still in flight land before the CTA leaves
+    mbar_wait_bounded(&sh.bar, 0);  // copies still in flight land before the block moves on
     return;
   }
   if (u >= live) return;
@@ -1028,7 +1070,7 @@ __global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
   for (int j = 0; j < LN; j++) {
     if (EXACT || j < Lr) {
       const EcVal t = tv[j];
-      const float2 x = sg[j * EC_THREADS + (int)(((unsigned)t.rot + (unsigned)i * t.ai) & (unsigned)(G - 1))];
+      const float2 x = sg[j * NTH + (int)(((unsigned)t.rot + (unsigned)i * t.ai) & (unsigned)(G - 1))];
       re[j] = x.x * t.gx + x.y * t.gy;
       im[j] = x.x * t.gy - x.y * t.gx;
     } else {
@@ -1041,6 +1083,21 @@ __global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
   const long o = (long)slot * d.out_stride + h0 + threadIdx.x;
   d.out_idx[o] = (int)(((unsigned)sh.grp[u] + S * (unsigned)i) * (unsigned)d.W + (unsigned)sh.res[u]);
   ((float2 *)d.out_val)[o] = make_float2(mre, mim);
+}
+
+__device__ __forceinline__ long ec_total(const V12Dev &d, int slot) {
+  return min((long)d.counters[slot * CNT_STRIDE + CNT_COMB] * (d.n / d.W), (long)d.out_cap);
+}
+
+template <int LN, bool EXACT>
+__global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
+  extern __shared__ __align__(128) float2 seg[];   // [loop][EC_THREADS]
+  __shared__ EcShared<EC_THREADS> sh;
+  const int slot = blockIdx.y;
+  if (blockIdx.x == 0 && threadIdx.x == 0) publish_count(d, slot, cand_total(d, slot));
+  const long total = ec_total(d, slot), h0 = (long)blockIdx.x * EC_THREADS;
+  if (h0 >= total) return;
+  ec32_block<LN, EXACT, EC_THREADS>(d, slot, h0, total, seg, sh);
 }
 
 // ---------------------------------------------------------------- scatter --
@@ -1253,6 +1310,260 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
   mark(se, s);
   note_launches(3);
   return cudaSuccess;
+}
+
+// ------------------------------------------------- persistent executor --
+//
+// sfft_exec_many over plans of different (n, k) as one kernel launch.  Each
+// CTA (PT threads, one per SM) takes items from a global queue in list
+// order.  An item is one block's worth of one stage of one signal -- a comb
+// sampling, a chunk of the fold, the comb residue list, one loop's bucket
+// FFT and selection, a chunk of the voting, a chunk of the estimation --
+// and runs the same device code as the stage kernels.  Before it starts, its
+// CTA waits (bounded) until the signal's counters show the stages it reads
+// complete; after it ends, the CTA bumps the counter of its own stage.  The
+// list is ordered so that every item's dependencies come earlier: a CTA only
+// waits for items that CTAs already took, and those wait only for earlier
+// items, so the queue always progresses, whatever the number of resident
+// CTAs.  A wait that runs out flags the signal (ERR_WAIT_TIMEOUT) and the
+// item is skipped, so the kernel always ends.
+
+constexpr int PT = 1024;                 // threads of the executor's CTA
+constexpr long PERSIST_POLLS = 1L << 24;  // polls of a dependency (with back-off)
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Waits until *p >= target.  Bounded; gives up at once when another wait of
+// the run has already run out (*abort), so a fault costs one time limit.
+__device__ __forceinline__ bool persist_wait(const int *p, int target, int *abort) {
+  for (long i = 0; i < PERSIST_POLLS; i++) {
+    if (ld_acquire(p) >= target) return true;
+    if ((i & 255) == 255 && *(volatile int *)abort) return false;
+    __nanosleep(64);
+  }
+  atomicExch(abort, 1);
+  return false;
+}
+
+__device__ __forceinline__ void mbar_inval(unsigned long long *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int LN, bool EX>
+__device__ __forceinline__ void persist_est(const V12Dev &d, const PersistGroup &g, int slot, int idx, float2 *seg,
+                                            EcShared<PT> &ecsh) {
+  if (g.est_comb) {
+    const long total = ec_total(d, slot), h0 = (long)idx * PT;
+    if (h0 < total) ec32_block<LN, EX, PT>(d, slot, h0, total, seg, ecsh);
+    __syncthreads();  // the item's mbarrier is no longer read
+    if (threadIdx.x == 0 && h0 < total) mbar_inval(&ecsh.bar);
+  } else {
+    const long total = min(cand_total(d, slot), (long)d.out_cap);
+    for (int c = 0; c < g.est_chunks; c++) {
+      const long h = ((long)idx * g.est_chunks + c) * PT + threadIdx.x;
+      if (h < total) est32_candidate<LN, EX>(d, slot, h);
+    }
+  }
+}
+
+__device__ __noinline__ void persist_est_any(const V12Dev &d, const PersistGroup &g, int slot, int idx, float2 *seg,
+                                             EcShared<PT> &ecsh) {
+  switch (d.L) {
+#define SFFT_PL(v)                                       \
+  case v:                                                \
+    persist_est<v, true>(d, g, slot, idx, seg, ecsh);    \
+    break;
+    SFFT_PL(8) SFFT_PL(9) SFFT_PL(10) SFFT_PL(11) SFFT_PL(12) SFFT_PL(13) SFFT_PL(14) SFFT_PL(15) SFFT_PL(16)
+    SFFT_PL(17) SFFT_PL(18) SFFT_PL(19) SFFT_PL(20) SFFT_PL(21) SFFT_PL(22) SFFT_PL(23) SFFT_PL(24)
+#undef SFFT_PL
+    default:
+      persist_est<32, false>(d, g, slot, idx, seg, ecsh);
+  }
+}
+
+template <typename In>
+__global__ void __launch_bounds__(PT, 1) k_persist32(PersistProg p) {
+  extern __shared__ __align__(128) unsigned char psmem[];
+  __shared__ PersistGroup sg;      // the plan of the current item
+  __shared__ EcShared<PT> ecsh;
+  __shared__ PersistItem sitem;
+  __shared__ int s_ok;
+  int *head = p.state, *abort = p.state + 1, *dep = p.state + 2;
+  int cached = -1;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int it = atomicAdd(head, 1);
+      sitem = it < p.nitems ? p.items[it] : PersistItem{-1, -1, 0, 0};
+    }
+    __syncthreads();
+    const PersistItem w = sitem;
+    if (w.kind < 0) break;
+    if (w.group != cached) {
+      const int *src = (const int *)(p.groups + w.group);
+      int *dst = (int *)&sg;
+      for (int i = threadIdx.x; i < (int)(sizeof(PersistGroup) / sizeof(int)); i += PT) dst[i] = src[i];
+      cached = w.group;
+      __syncthreads();
+    }
+    const V12Dev &d = sg.d;
+    int *sdep = dep + 4 * (sg.gslot0 + w.slot);
+    if (threadIdx.x == 0) {
+      bool ok = !*(volatile int *)abort;
+      if (ok && w.kind == PK_LIST)
+        ok = persist_wait(sdep + 0, d.comb_loops, abort);
+      else if (ok && w.kind == PK_BUCKET)
+        ok = persist_wait(sdep + 1, sg.nfold, abort);
+      else if (ok && (w.kind == PK_VOTE || w.kind == PK_EST))
+        ok = persist_wait(sdep + 2, d.L, abort) && persist_wait(sdep + 3, 1, abort);
+      if (!ok) atomicOr(&d.counters[w.slot * CNT_STRIDE + CNT_ERR], ERR_WAIT_TIMEOUT);
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (s_ok) {
+      switch (w.kind) {
+        case PK_COMB:
+          if (sg.per_comb == 1)
+            comb_block<float, 1, In>(d, w.idx, w.slot, psmem);
+          else if (sg.per_comb == 2)
+            comb_block<float, 2, In>(d, w.idx, w.slot, psmem);
+          else
+            comb_block<float, 4, In>(d, w.idx, w.slot, psmem);
+          break;
+        case PK_FOLD:
+          for (int c = 0; c < sg.fold_chunks; c++)
+            fold_split_thread<In, 4>(d, w.slot, ((long)w.idx * sg.fold_chunks + c) * PT + threadIdx.x);
+          break;
+        case PK_LIST:
+          comb_list_block(d, w.slot);
+          break;
+        case PK_BUCKET:
+          if (sg.per_bucket == 1)
+            bucket_block<float, 1>(d, w.idx, w.slot, psmem);
+          else if (sg.per_bucket == 2)
+            bucket_block<float, 2>(d, w.idx, w.slot, psmem);
+          else
+            bucket_block<float, 4>(d, w.idx, w.slot, psmem);
+          break;
+        case PK_VOTE:
+          for (int c = 0; c < sg.vote_chunks; c++)
+            vote_comb_thread(d, sg.vote_cmax, w.slot, ((long)w.idx * sg.vote_chunks + c) * PT + threadIdx.x);
+          break;
+        default:  // PK_EST
+          if (w.idx == 0 && threadIdx.x == 0) publish_count(d, w.slot, cand_total(d, w.slot));
+          persist_est_any(d, sg, w.slot, w.idx, (float2 *)psmem, ecsh);
+      }
+    }
+    __syncthreads();  // the item's writes precede its completion count
+    if (threadIdx.x == 0) {
+      const int k = w.kind == PK_COMB ? 0 : w.kind == PK_FOLD ? 1 : w.kind == PK_BUCKET ? 2 : w.kind == PK_LIST ? 3 : -1;
+      if (k >= 0) {
+        __threadfence();
+        atomicAdd(sdep + k, 1);
+      }
+    }
+  }
+}
+
+bool persist_eligible(const V12Dev &d) {
+  const int mx = v12_max_fft(PREC_FP32);
+  return d.version == 1 && !d.voted && d.prec == PREC_FP32 && !d.large_buckets && !d.large_comb && d.L <= 32 &&
+         d.W <= mx && d.B_loc <= mx && d.B_est <= mx && d.comb_loops <= 64;
+}
+
+static int per_of(int N) {
+  const int per = (N / 4 + PT - 1) / PT;
+  return per <= 1 ? 1 : per <= 2 ? 2 : 4;
+}
+
+void persist_shape(PersistGroup &g) {
+  V12Dev &d = g.d;
+  if (d.xs_perm && d.L > 24) d.xs_perm = 0;  // the comb-residue items hold L x PT values in shared memory
+  g.per_comb = per_of(d.W);
+  g.per_bucket = per_of(std::max(d.B_loc, d.B_est));
+  g.fold_chunks = 8;
+  g.nfold = (int)((d.xs_size * 4 + (long)PT * g.fold_chunks - 1) / ((long)PT * g.fold_chunks));
+  g.vote_cmax = (int)std::min<long>(d.W, (long)d.comb_loops * d.num);
+  g.vote_chunks = 8;
+  const long votes = (long)d.num * g.vote_cmax * d.L_loc;
+  g.nvote = (int)((votes + (long)PT * g.vote_chunks - 1) / ((long)PT * g.vote_chunks));
+  const long cands = std::min<long>((long)g.vote_cmax * (d.n / d.W), (long)d.out_cap);
+  g.est_comb = d.xs_perm != 0;
+  g.est_chunks = g.est_comb ? 1 : 4;
+  g.nest = (int)((cands + (long)PT * g.est_chunks - 1) / ((long)PT * g.est_chunks));
+}
+
+size_t persist_smem(const PersistGroup *groups, int ngroups) {
+  size_t m = 0;
+  for (int i = 0; i < ngroups; i++) {
+    const V12Dev &d = groups[i].d;
+    m = std::max(m, BucketSmem<float>::bytes(std::max(d.W, std::max(d.B_loc, d.B_est)), d.num));
+    if (groups[i].est_comb) m = std::max(m, sizeof(float2) * (size_t)PT * d.L);
+  }
+  return m;
+}
+
+// Signals in decreasing order of work; stage s of the signal ranked r has
+// priority r + lag(s), lags increasing along the dependency chain.
+void persist_items(const PersistGroup *groups, int ngroups, std::vector<PersistItem> &items) {
+  struct Sig {
+    int g, s;
+    double work;
+  };
+  std::vector<Sig> sigs;
+  for (int g = 0; g < ngroups; g++)
+    for (int s = 0; s < groups[g].slots; s++)
+      sigs.push_back({g, s, (double)groups[g].d.xs_size * groups[g].d.L + (double)groups[g].nest * PT});
+  std::stable_sort(sigs.begin(), sigs.end(), [](const Sig &a, const Sig &b) { return a.work > b.work; });
+  struct Key {
+    long prio;
+    int kind;
+    long seq;
+    PersistItem it;
+  };
+  std::vector<Key> keys;
+  long seq = 0;
+  auto add = [&](long prio, int kind, const PersistItem &it) { keys.push_back({prio, kind, seq++, it}); };
+  for (size_t r = 0; r < sigs.size(); r++) {
+    const PersistGroup &G = groups[sigs[r].g];
+    const int g = sigs[r].g, s = sigs[r].s;
+    const long base = (long)r;
+    for (int c = 0; c < G.d.comb_loops; c++) add(base, PK_COMB, {PK_COMB, g, s, c});
+    for (int i = 0; i < G.nfold; i++) add(base, PK_FOLD, {PK_FOLD, g, s, i});
+    add(base + 2, PK_LIST, {PK_LIST, g, s, 0});
+    for (int j = 0; j < G.d.L; j++) add(base + 2, PK_BUCKET, {PK_BUCKET, g, s, j});
+    for (int i = 0; i < G.nvote; i++) add(base + 4, PK_VOTE, {PK_VOTE, g, s, i});
+    for (int i = 0; i < G.nest; i++) add(base + 4, PK_EST, {PK_EST, g, s, i});
+  }
+  std::stable_sort(keys.begin(), keys.end(), [](const Key &a, const Key &b) {
+    if (a.prio != b.prio) return a.prio < b.prio;
+    if (a.kind != b.kind) return a.kind < b.kind;
+    return a.seq < b.seq;
+  });
+  items.clear();
+  items.reserve(keys.size());
+  for (const Key &k : keys) items.push_back(k.it);
+}
+
+cudaError_t persist_run(const PersistProg &p, cudaStream_t s) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(p.state, 0, sizeof(int) * (2 + 4 * (size_t)p.nslots_total), s))) return e;
+  const int grid = sm_count();
+  // always opted in: with the kernel's static shared memory, 32-48 KB of
+  // dynamic shared memory would exceed the default limit
+  const size_t sm = std::max<size_t>(p.smem, 40 * 1024);
+  if (p.in_type == IN_C128) {
+    if ((e = set_smem(k_persist32<double2>, sm))) return e;
+    k_persist32<double2><<<grid, PT, sm, s>>>(p);
+  } else {
+    if ((e = set_smem(k_persist32<float2>, sm))) return e;
+    k_persist32<float2><<<grid, PT, sm, s>>>(p);
+  }
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t global_fft_c128(void *a, void *b, int N, int narr, long arr_stride, long slot_stride, int nslots,

@@ -92,7 +92,7 @@ class MixedBatch:
     graph per call; tune as in Server (2: autotuned, k rounded to its
     bucket)."""
 
-    def __init__(self, shapes, tune=0, complex64=False, device=-1):
+    def __init__(self, shapes, tune=0, complex64=False, device=-1, persistent=False):
         self._L = _lib.load()
         self.shapes = [(int(n), int(k), int(v), p) for n, k, v, p in shapes]
         num = len(self.shapes)
@@ -106,6 +106,8 @@ class MixedBatch:
         if not self._m:
             raise RuntimeError("sfft_mixed_create failed: " + _lib.last_error())
         self.plans = int(self._L.sfft_mixed_groups(self._m))
+        if persistent and self._L.sfft_mixed_set_persistent(self._m, 1) != 0:
+            raise RuntimeError("sfft_mixed_set_persistent failed: " + _lib.last_error())
 
     def run(self, signals, seeds=None):
         """One execution over device tensors (one per shape), asynchronous."""

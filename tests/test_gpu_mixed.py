@@ -155,3 +155,81 @@ def test_mixed_rejects_bad_shapes(env):
     arr = lambda j: (ctypes.c_int * num)(*[s[j] for s in bad])
     assert not L.sfft_mixed_create(num, arr(0), arr(1), arr(2), arr(3), 0, 1, -1)
     assert _lib.last_error()
+
+
+def _uneven_shapes(count, seed0=0):
+    """(n, k) of an uneven v2 batch: n log-uniform over 2^16..2^22, k uniform
+    in [10, 500] (the bench's uneven workload, fewer signals)."""
+    out = []
+    for s in range(seed0, seed0 + count):
+        r = np.random.default_rng(s)
+        out.append((1 << int(r.integers(16, 23)), int(r.integers(10, 501))))
+    return out
+
+
+def _create_tuned(L, _lib, sigs, persistent):
+    num = len(sigs)
+    arr = lambda j: (ctypes.c_int * num)(*[s[j] for s in sigs])
+    m = L.sfft_mixed_create(num, arr(0), arr(1), arr(2), arr(3), 0, 2, -1)
+    assert m, _lib.last_error()
+    if persistent:
+        assert L.sfft_mixed_set_persistent(m, 1) == 0, _lib.last_error()
+    return m
+
+
+def test_persistent_executor_equals_graph(env):
+    """The persistent executor (one kernel over a device work queue) must
+    give every FP32 v2 signal exactly the result of the per-plan graph
+    branches -- the same arithmetic per candidate -- on the direct first call
+    and on graph replays, and the groups it does not take (v1, v3, FP64)
+    still run as branches of the same graph."""
+    torch, _lib, L, O = env
+    from sfft_gb300 import signals
+    shapes = _uneven_shapes(24, seed0=40)
+    sigs = [(n, k, V2, FP32) for n, k in shapes]
+    sigs += [(1 << 16, 50, V1, FP64), (1 << 16, 50, V3, FP64), (1 << 17, 64, V2, FP64),
+             (1 << 22, 500, V2, FP32), (1 << 16, 500, V2, FP32)]   # comb of 16384; 16 candidates per residue
+    data = [signals.make_signal_torch(n, k, 900 + i, snr_db=40.0) for i, (n, k, _, _) in enumerate(sigs)]
+    xs = [x for x, _, _ in data]
+    torch.cuda.synchronize()
+    mg = _create_tuned(L, _lib, sigs, False)
+    mp = _create_tuned(L, _lib, sigs, True)
+    for call, seeds in enumerate(([3 + i for i in range(len(sigs))], [77 + 5 * i for i in range(len(sigs))])):
+        before = L.sfft_kernel_launches()
+        _run(L, _lib, mp, xs, seeds)
+        launches_p = L.sfft_kernel_launches() - before
+        before = L.sfft_kernel_launches()
+        _run(L, _lib, mg, xs, seeds)
+        launches_g = L.sfft_kernel_launches() - before
+        if call == 0:
+            # the direct first call: the executor plus the branches of the three
+            # groups it does not take, against a branch per group
+            assert launches_p < launches_g / 3, (launches_p, launches_g)
+        for s, sig in enumerate(sigs):
+            gi, gv = _result(torch, _lib, L, mg, s)
+            pi, pv = _result(torch, _lib, L, mp, s)
+            np.testing.assert_array_equal(pi, gi, err_msg=f"call {call}, signal {s} {sig}")
+            if sig[2] == V3:
+                assert np.max(np.abs(pv - gv), initial=0) <= 1e-10 * max(1.0, np.max(np.abs(gv), initial=0))
+            else:
+                np.testing.assert_array_equal(pv, gv, err_msg=f"call {call}, signal {s} {sig}")
+    L.sfft_mixed_destroy(mg)
+    L.sfft_mixed_destroy(mp)
+
+
+def test_persistent_executor_alone_is_one_launch(env):
+    """An all-FP32 v2 batch runs as exactly one kernel launch per call."""
+    torch, _lib, L, O = env
+    from sfft_gb300 import signals
+    sigs = [(n, k, V2, FP32) for n, k in _uneven_shapes(12, seed0=7)]
+    xs = [signals.make_signal_torch(n, k, 300 + i, snr_db=40.0)[0] for i, (n, k, _, _) in enumerate(sigs)]
+    torch.cuda.synchronize()
+    m = _create_tuned(L, _lib, sigs, True)
+    before = L.sfft_kernel_launches()
+    _run(L, _lib, m, xs, list(range(len(sigs))))
+    assert L.sfft_kernel_launches() - before == 1
+    _run(L, _lib, m, xs, list(range(len(sigs))))     # a graph replay
+    for s, (n, k, _, _) in enumerate(sigs):
+        gi, gv = _result(torch, _lib, L, m, s)
+        assert gi.size > 0
+    L.sfft_mixed_destroy(m)
