@@ -98,7 +98,7 @@ struct PersistGroup {
   int slots;         // its signals
   int per_comb, per_bucket;   // butterflies per thread of the comb / bucket FFTs (1, 2, 4)
   int fold_chunks;   // 1024-thread chunks of the fold per item
-  int vote_cmax, vote_chunks; // k_vote_comb's residue bound, 1024-thread chunks per item
+  int vote_cmax, vote_chunks; // comb residues at most; unused (1)
   int est_comb;      // 1: estimation by comb residue (1024 candidates per item), 0: random lookups
   int est_chunks;    // random lookups: 1024-candidate chunks per item
   int nfold, nvote, nest;     // items per signal of those stages
@@ -116,8 +116,9 @@ struct PersistProg {
   size_t smem;                 // dynamic shared memory per CTA
   int in_type;
 };
-// Dependency-ordered item list for `groups` (host copies; d must be set).
-void persist_items(const PersistGroup *groups, int ngroups, std::vector<PersistItem> &items);
+// Dependency-ordered item list for `groups` (host copies; d must be set),
+// ordered for `workers` resident CTAs.
+void persist_items(const PersistGroup *groups, int ngroups, std::vector<PersistItem> &items, int workers);
 // Shared memory the executor needs for these groups, and whether a plan
 // view qualifies (plain FP32 v2, FFTs in shared memory, at most 32 loops).
 size_t persist_smem(const PersistGroup *groups, int ngroups);

@@ -287,7 +287,12 @@ int sfft_mixed_set_persistent(sfft_mixed *m, int on) {
     pg.push_back(p);
   }
   std::vector<sfft::PersistItem> items;
-  sfft::persist_items(pg.data(), (int)pg.size(), items);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device) != cudaSuccess || sms <= 0) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  sfft::persist_items(pg.data(), (int)pg.size(), items, sms);
   const size_t smem = sfft::persist_smem(pg.data(), (int)pg.size());
   if (smem > 200 * 1024) {  // with the executor's static shared memory, above a CTA's 227 KB
     for (Group &g : m->groups) g.persist = false;

@@ -15,6 +15,8 @@
 // batch of signals sharing a plan.  FP64 instantiations reproduce the CPU
 // definition bit for bit; FP32 ones accumulate in float.
 #include <algorithm>
+#include <functional>
+#include <queue>
 #include <cstdlib>
 #include <tuple>
 #include <mutex>
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(256) k_fold(V12Dev d) {
 // instead of several signals' inputs contending for L2 and being fetched
 // from DRAM repeatedly.  The summation order differs from the reference's,
 // which the FP32 form does not reproduce anyway.
-template <typename In, int S>
+template <typename In, int S, int U = 4>
 __device__ __forceinline__ void fold_split_thread(const V12Dev &d, int slot, long gt) {
   const long g = gt / S;
   const int part = (int)(gt % S);
@@ -128,10 +130,10 @@ __device__ __forceinline__ void fold_split_thread(const V12Dev &d, int slot, lon
     const unsigned ai = (unsigned)rp[d.L + j], mask = (unsigned)d.n - 1u;
     const In *x = (const In *)d.inputs[slot];
     const int step = S * B;
-    for (int t0 = b + part * B; t0 < w; t0 += 4 * step) {
-      float2 xv[4], hv[4];
+    for (int t0 = b + part * B; t0 < w; t0 += U * step) {  // U gathers in flight
+      float2 xv[U], hv[U];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
+      for (int u = 0; u < U; u++) {
         const int t = t0 + u * step;
         if (t < w) {
           xv[u] = cvt_in<float>(__ldg(x + (((unsigned)t * ai) & mask)));
@@ -139,7 +141,7 @@ __device__ __forceinline__ void fold_split_thread(const V12Dev &d, int slot, lon
         }
       }
 #pragma unroll
-      for (int u = 0; u < 4; u++)
+      for (int u = 0; u < U; u++)
         if (t0 + u * step < w) acc = cadd<float>(acc, cmul<float>(xv[u], hv[u]));
     }
   }
@@ -238,15 +240,15 @@ __global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) { comb_list_block(
 // One vote for frequency f: the counter is (epoch << 8) | votes, so a
 // counter from an earlier execution restarts at 1.  The vote that reaches
 // the threshold records the frequency (v1, and v2 in the voted mode).
+// Tags only grow between clears of the counters, so an atomic max with
+// (epoch << 8) resets a counter of an earlier execution to zero votes and
+// leaves one of this execution alone; the atomic add that follows (same
+// address, same thread: ordered after it) returns this vote's count.  One
+// round trip, no compare-and-swap loop.
 __device__ __forceinline__ void vote_one(const V12Dev &d, int slot, unsigned f, unsigned ep, unsigned *score,
                                          int *cnt) {
-  unsigned cur = score[f], nv;
-  for (;;) {
-    nv = ((cur >> 8) == ep) ? cur + 1u : ((ep << 8) | 1u);
-    const unsigned prev = atomicCAS(&score[f], cur, nv);
-    if (prev == cur) break;
-    cur = prev;
-  }
+  atomicMax(&score[f], ep << 8);
+  const unsigned nv = atomicAdd(&score[f], 1u) + 1u;
   if ((int)(nv & 255u) == d.thresh) {
     atomicAdd(&cnt[CNT_VOTED], 1);
     if (d.version == 0 || d.voted) {
@@ -289,13 +291,16 @@ __global__ void __launch_bounds__(256) k_vote(V12Dev d) {
   }
 }
 
-// v2 voting by enumeration: for selected bucket J and comb residue r, the
-// positions p of J's range whose frequency p a mod n lies in residue class r
-// mod W are p = c (mod W) with c = r a^-1 mod W (a odd; W divides n) -- one
-// thread per (loop, bucket, residue) visits exactly those, instead of one
-// thread per position testing the residue bitmap.  Same votes, any order.
-__device__ __forceinline__ void vote_comb_thread(const V12Dev &d, int cmax, int slot, long g) {
+// v2 voting by residue enumeration: for selected bucket J and comb residue
+// r, the positions p of J's range whose frequency p a mod n lies in residue
+// class r mod W are p = c (mod W) with c = r a^-1 mod W -- one thread per
+// (loop, bucket, residue) visits exactly those.  Cheaper than the bitmap
+// walk below when the residues are few against the bucket width (many
+// light threads instead of a few threads with several votes each).
+__global__ void __launch_bounds__(256) k_vote_comb(V12Dev d, int cmax) {
+  const int slot = blockIdx.y;
   const long per_loop = (long)d.num * cmax;
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= per_loop * d.L_loc) return;
   const int j = (int)(g / per_loop);
   const long e = g - (long)j * per_loop;
@@ -318,8 +323,60 @@ __device__ __forceinline__ void vote_comb_thread(const V12Dev &d, int cmax, int 
   }
 }
 
-__global__ void __launch_bounds__(256) k_vote_comb(V12Dev d, int cmax) {
-  vote_comb_thread(d, cmax, blockIdx.y, (long)blockIdx.x * blockDim.x + threadIdx.x);
+// v2 voting by comb-key bitmap.  In location loop j a position p votes iff
+// its frequency p a mod n lies in an approved comb residue class, i.e. iff
+// p mod W is in K_j = {r ai mod W : r approved} (a ai = 1 mod W, W | n).  A
+// block builds K_j as a W-bit bitmap in shared memory; then each thread
+// takes 32 consecutive positions of one selected bucket's range at a time:
+// the 32 bits starting at (low + o) mod W (two words, funnel shift) name
+// exactly the positions that vote.  The reference walks the approved
+// residues in the same way through sorted (residue, key) pairs
+// (computefourier-1.0-2.0.cc:125-184); the votes are the same, in any order.
+constexpr int VB_BUCKETS = 64;   // selected buckets per block
+
+__device__ __forceinline__ void vote_bits_block(const V12Dev &d, int j, int i0, int slot, unsigned *kb) {
+  const int W = d.W, nw = W >> 5, L = d.L;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const unsigned a = (unsigned)rp[j], ai = (unsigned)rp[L + j];
+  const unsigned ep = (unsigned)rp[2 * L + d.comb_loops];
+  const unsigned mask = (unsigned)d.n - 1u, wm = (unsigned)W - 1u;
+  int *cnt = d.counters + slot * CNT_STRIDE;
+  for (int w = threadIdx.x; w < nw; w += blockDim.x) kb[w] = 0u;
+  __syncthreads();
+  const int ncomb = cnt[CNT_COMB];
+  const int *list = d.comb_list + (long)slot * W;
+  for (int t = threadIdx.x; t < ncomb; t += blockDim.x) {
+    const unsigned c = ((unsigned)list[t] * ai) & wm;
+    atomicOr(&kb[c >> 5], 1u << (c & 31));
+  }
+  __syncthreads();
+  const int q = d.q_loc, nch = (q + 31) >> 5;
+  const int i1 = min(d.num, i0 + VB_BUCKETS);
+  const int tasks = (i1 - i0) * nch;
+  const int *Js = d.J + ((long)slot * L + j) * d.num;
+  unsigned *score = d.score + (long)slot * d.n;
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int i = i0 + t / nch, o0 = (t - (t / nch) * nch) << 5;
+    const unsigned low = ((unsigned)Js[i] * (unsigned)q - (unsigned)(q >> 1) + (unsigned)d.n) & mask;
+    const unsigned b0 = (low + (unsigned)o0) & wm;
+    const unsigned w0 = b0 >> 5;
+    unsigned word = __funnelshift_r(kb[w0], kb[(w0 + 1) & (unsigned)(nw - 1)], b0 & 31u);
+    const int rem = q - o0;
+    if (rem < 32) word &= (1u << rem) - 1u;
+    while (word) {
+      const int k = __ffs(word) - 1;
+      word &= word - 1u;
+      const unsigned p = (low + (unsigned)(o0 + k)) & mask;
+      vote_one(d, slot, (p * a) & mask, ep, score, cnt);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_vote_bits(V12Dev d) {
+  extern __shared__ unsigned vb_keys[];
+  const int nbc = (d.num + VB_BUCKETS - 1) / VB_BUCKETS;
+  const int j = blockIdx.x / nbc;
+  vote_bits_block(d, j, (blockIdx.x - j * nbc) * VB_BUCKETS, blockIdx.y, vb_keys);
 }
 
 // ---------------------------------------------------------------- bucket --
@@ -1295,9 +1352,14 @@ static cudaError_t run_typed(const V12Dev &d, int nslots, cudaStream_t s, StageE
   }
   {
     const long cmax = std::min<long>(d.W, (long)d.comb_loops * d.num);
-    if (d.version == 1 && cmax < d.q_loc) {
+    if (d.version == 1 && 4 * cmax < d.q_loc) {
       const long threads = (long)d.num * cmax * d.L_loc;
       k_vote_comb<<<dim3((unsigned)((threads + 255) / 256), nslots), 256, 0, s>>>(d, (int)cmax);
+    } else if (d.version == 1 && d.W >= 32) {
+      const int nbc = (d.num + VB_BUCKETS - 1) / VB_BUCKETS;
+      const size_t sm = sizeof(unsigned) * (size_t)(d.W >> 5);
+      if ((e = set_smem(k_vote_bits, sm))) return e;
+      k_vote_bits<<<dim3((unsigned)(d.L_loc * nbc), nslots), 256, sm, s>>>(d);
     } else {
       const long votes = ((long)d.num * d.q_loc) * d.L_loc;
       k_vote<<<dim3((unsigned)((votes + 255) / 256), nslots), 256, 0, s>>>(d);
@@ -1448,10 +1510,11 @@ __global__ void __launch_bounds__(PT, 1) k_persist32(PersistProg p) {
           else
             bucket_block<float, 4>(d, w.idx, w.slot, psmem);
           break;
-        case PK_VOTE:
-          for (int c = 0; c < sg.vote_chunks; c++)
-            vote_comb_thread(d, sg.vote_cmax, w.slot, ((long)w.idx * sg.vote_chunks + c) * PT + threadIdx.x);
+        case PK_VOTE: {  // loop j, buckets [i0, i0 + VB_BUCKETS)
+          const int nbc = (d.num + VB_BUCKETS - 1) / VB_BUCKETS, j = w.idx / nbc;
+          vote_bits_block(d, j, (w.idx - j * nbc) * VB_BUCKETS, w.slot, (unsigned *)psmem);
           break;
+        }
         default:  // PK_EST
           if (w.idx == 0 && threadIdx.x == 0) publish_count(d, w.slot, cand_total(d, w.slot));
           persist_est_any(d, sg, w.slot, w.idx, (float2 *)psmem, ecsh);
@@ -1471,7 +1534,7 @@ __global__ void __launch_bounds__(PT, 1) k_persist32(PersistProg p) {
 bool persist_eligible(const V12Dev &d) {
   const int mx = v12_max_fft(PREC_FP32);
   return d.version == 1 && !d.voted && d.prec == PREC_FP32 && !d.large_buckets && !d.large_comb && d.L <= 32 &&
-         d.W <= mx && d.B_loc <= mx && d.B_est <= mx && d.comb_loops <= 64;
+         d.W >= 32 && d.W <= mx && d.B_loc <= mx && d.B_est <= mx && d.comb_loops <= 64;
 }
 
 static int per_of(int N) {
@@ -1487,9 +1550,8 @@ void persist_shape(PersistGroup &g) {
   g.fold_chunks = 8;
   g.nfold = (int)((d.xs_size * 4 + (long)PT * g.fold_chunks - 1) / ((long)PT * g.fold_chunks));
   g.vote_cmax = (int)std::min<long>(d.W, (long)d.comb_loops * d.num);
-  g.vote_chunks = 8;
-  const long votes = (long)d.num * g.vote_cmax * d.L_loc;
-  g.nvote = (int)((votes + (long)PT * g.vote_chunks - 1) / ((long)PT * g.vote_chunks));
+  g.vote_chunks = 1;
+  g.nvote = d.L_loc * ((d.num + VB_BUCKETS - 1) / VB_BUCKETS);
   const long cands = std::min<long>((long)g.vote_cmax * (d.n / d.W), (long)d.out_cap);
   g.est_comb = d.xs_perm != 0;
   g.est_chunks = g.est_comb ? 1 : 4;
@@ -1506,9 +1568,15 @@ size_t persist_smem(const PersistGroup *groups, int ngroups) {
   return m;
 }
 
-// Signals in decreasing order of work; stage s of the signal ranked r has
-// priority r + lag(s), lags increasing along the dependency chain.
-void persist_items(const PersistGroup *groups, int ngroups, std::vector<PersistItem> &items) {
+// The queue order comes from a simulation of the executor on `workers`
+// CTAs: every item gets a rough duration, becomes ready when the stages it
+// reads are complete, and a free CTA takes the ready item of the
+// highest-ranked signal (signals ranked by decreasing work), later stages
+// first.  The items in simulated start order form the queue: an item starts
+// only after its dependencies finished, so they precede it in the queue,
+// and the order keeps CTAs off dependency waits as far as the durations
+// are right.
+void persist_items(const PersistGroup *groups, int ngroups, std::vector<PersistItem> &items, int workers) {
   struct Sig {
     int g, s;
     double work;
@@ -1518,34 +1586,104 @@ void persist_items(const PersistGroup *groups, int ngroups, std::vector<PersistI
     for (int s = 0; s < groups[g].slots; s++)
       sigs.push_back({g, s, (double)groups[g].d.xs_size * groups[g].d.L + (double)groups[g].nest * PT});
   std::stable_sort(sigs.begin(), sigs.end(), [](const Sig &a, const Sig &b) { return a.work > b.work; });
-  struct Key {
-    long prio;
-    int kind;
-    long seq;
-    PersistItem it;
+  // durations (microseconds of one CTA, rough)
+  auto dur = [&](const PersistGroup &G, int kind) -> double {
+    const V12Dev &d = G.d;
+    switch (kind) {
+      case PK_COMB: return 2.0 + d.W / 2048.0;
+      case PK_FOLD: {
+        const double taps = (double)PT * G.fold_chunks / 4.0 * ((double)d.w_loc / d.B_loc + (double)d.w_est / d.B_est) / 2;
+        return 1.0 + taps / 700.0;
+      }
+      case PK_LIST: return 1.0;
+      case PK_BUCKET: return 2.0 + std::max(d.B_loc, d.B_est) / 2048.0;
+      case PK_VOTE: return 1.0 + (double)VB_BUCKETS * ((d.q_loc + 31) / 32) / 512.0;
+      default: return 1.0 + (double)PT * G.est_chunks * d.L / 4000.0;
+    }
   };
-  std::vector<Key> keys;
-  long seq = 0;
-  auto add = [&](long prio, int kind, const PersistItem &it) { keys.push_back({prio, kind, seq++, it}); };
-  for (size_t r = 0; r < sigs.size(); r++) {
-    const PersistGroup &G = groups[sigs[r].g];
-    const int g = sigs[r].g, s = sigs[r].s;
-    const long base = (long)r;
-    for (int c = 0; c < G.d.comb_loops; c++) add(base, PK_COMB, {PK_COMB, g, s, c});
-    for (int i = 0; i < G.nfold; i++) add(base, PK_FOLD, {PK_FOLD, g, s, i});
-    add(base + 2, PK_LIST, {PK_LIST, g, s, 0});
-    for (int j = 0; j < G.d.L; j++) add(base + 2, PK_BUCKET, {PK_BUCKET, g, s, j});
-    for (int i = 0; i < G.nvote; i++) add(base + 4, PK_VOTE, {PK_VOTE, g, s, i});
-    for (int i = 0; i < G.nest; i++) add(base + 4, PK_EST, {PK_EST, g, s, i});
-  }
-  std::stable_sort(keys.begin(), keys.end(), [](const Key &a, const Key &b) {
-    if (a.prio != b.prio) return a.prio < b.prio;
+  const int nsig = (int)sigs.size();
+  // per signal: items per stage, remaining counts, completion times
+  struct St {
+    int comb_left, fold_left, bucket_left, list_left;
+    double comb_done, fold_done, bucket_done, list_done;
+    bool list_q, bucket_q, tail_q;
+  };
+  std::vector<St> st(nsig);
+  struct Ready {
+    double t;
+    int rank, kind, idx;
+  };
+  // ready items: ordered by (rank, later kind first, idx) among those ready by now
+  auto cmp = [](const Ready &a, const Ready &b) {
+    if (a.rank != b.rank) return a.rank > b.rank;
     if (a.kind != b.kind) return a.kind < b.kind;
-    return a.seq < b.seq;
-  });
+    return a.idx > b.idx;
+  };
+  std::priority_queue<Ready, std::vector<Ready>, decltype(cmp)> ready(cmp);
+  auto later = [](const Ready &a, const Ready &b) { return a.t > b.t; };
+  std::priority_queue<Ready, std::vector<Ready>, decltype(later)> pending(later);  // not ready yet
+  for (int r = 0; r < nsig; r++) {
+    const PersistGroup &G = groups[sigs[r].g];
+    st[r] = {G.d.comb_loops, G.nfold, G.d.L, 1, 0, 0, 0, 0, false, false, false};
+    for (int c = 0; c < G.d.comb_loops; c++) ready.push({0.0, r, PK_COMB, c});
+    for (int i = 0; i < G.nfold; i++) ready.push({0.0, r, PK_FOLD, i});
+  }
+  std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
+  for (int w = 0; w < std::max(1, workers); w++) free_at.push(0.0);
   items.clear();
-  items.reserve(keys.size());
-  for (const Key &k : keys) items.push_back(k.it);
+  auto release = [&](int r, double t) {  // newly ready stages of signal r at time t
+    St &x = st[r];
+    const PersistGroup &G = groups[sigs[r].g];
+    if (!x.list_q && x.comb_left == 0) {
+      x.list_q = true;
+      pending.push({t, r, PK_LIST, 0});
+    }
+    if (!x.bucket_q && x.fold_left == 0) {
+      x.bucket_q = true;
+      for (int j = 0; j < G.d.L; j++) pending.push({t, r, PK_BUCKET, j});
+    }
+    if (!x.tail_q && x.bucket_left == 0 && x.list_left == 0) {
+      x.tail_q = true;
+      for (int i = 0; i < G.nvote; i++) pending.push({t, r, PK_VOTE, i});
+      for (int i = 0; i < G.nest; i++) pending.push({t, r, PK_EST, i});
+    }
+  };
+  while (!ready.empty() || !pending.empty()) {
+    double t = free_at.top();
+    free_at.pop();
+    while (!pending.empty() && pending.top().t <= t) {
+      ready.push(pending.top());
+      pending.pop();
+    }
+    if (ready.empty()) {  // idle until the next item becomes ready
+      t = pending.top().t;
+      while (!pending.empty() && pending.top().t <= t) {
+        ready.push(pending.top());
+        pending.pop();
+      }
+    }
+    const Ready it = ready.top();
+    ready.pop();
+    const int g = sigs[it.rank].g, sl = sigs[it.rank].s;
+    const double end = t + dur(groups[g], it.kind);
+    items.push_back({it.kind, g, sl, it.idx});
+    free_at.push(end);
+    St &x = st[it.rank];
+    // completion bookkeeping (dependents become ready when the last item of a stage ends)
+    if (it.kind == PK_COMB) {
+      x.comb_done = std::max(x.comb_done, end);
+      if (--x.comb_left == 0) release(it.rank, x.comb_done);
+    } else if (it.kind == PK_FOLD) {
+      x.fold_done = std::max(x.fold_done, end);
+      if (--x.fold_left == 0) release(it.rank, x.fold_done);
+    } else if (it.kind == PK_BUCKET) {
+      x.bucket_done = std::max(x.bucket_done, end);
+      if (--x.bucket_left == 0) release(it.rank, std::max(x.bucket_done, x.list_done));
+    } else if (it.kind == PK_LIST) {
+      x.list_done = end;
+      if (--x.list_left == 0) release(it.rank, std::max(x.bucket_done, x.list_done));
+    }
+  }
 }
 
 cudaError_t persist_run(const PersistProg &p, cudaStream_t s) {
