@@ -152,7 +152,7 @@ def test_exec_many_sparse_matches_sequential_oracle(env, oracle_lib):
         op = oracle_lib.OraclePlan(n, k, v - 1)
         oracle_lib.seed_libc(91)
         refs = [op.exec(x) for x in xs]
-        p = sfft(n, k, v, max_batch=2)              # chunks of 2: four pipelined chunks
+        p = sfft(n, k, v, max_batch=2)              # one signal per chunk: seven pipelined chunks
         cap = p.capacity
         nb = n * 16
         hin = [L.sfft_malloc(nb) for _ in range(num)]
