@@ -1043,7 +1043,19 @@ def copy_bandwidth(nbytes=1 << 30, reps=5):
         e1.record()
         e1.synchronize()
         out[name] = reps * nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9
-    del h, d
+    # both directions at once, on two streams (what the dense e2e leg needs)
+    h2, d2 = torch.empty_like(h).pin_memory(), torch.empty_like(d)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+    torch.cuda.synchronize()
+    out["bidirectional_total_gbs"] = 2 * reps * nbytes / (time.perf_counter() - t0) / 1e9
+    del h, d, h2, d2
     torch.cuda.empty_cache()
     return out
 

@@ -167,10 +167,10 @@ def _uneven_shapes(count, seed0=0):
     return out
 
 
-def _create_tuned(L, _lib, sigs, persistent):
+def _create_tuned(L, _lib, sigs, persistent, in_type=0):
     num = len(sigs)
     arr = lambda j: (ctypes.c_int * num)(*[s[j] for s in sigs])
-    m = L.sfft_mixed_create(num, arr(0), arr(1), arr(2), arr(3), 0, 2, -1)
+    m = L.sfft_mixed_create(num, arr(0), arr(1), arr(2), arr(3), in_type, 2, -1)
     assert m, _lib.last_error()
     if persistent:
         assert L.sfft_mixed_set_persistent(m, 1) == 0, _lib.last_error()
@@ -233,3 +233,26 @@ def test_persistent_executor_alone_is_one_launch(env):
         gi, gv = _result(torch, _lib, L, m, s)
         assert gi.size > 0
     L.sfft_mixed_destroy(m)
+
+
+def test_persistent_executor_complex64_inputs(env):
+    """complex64 inputs (the executor's other instantiation) give the same
+    results through the executor as through the graph branches."""
+    torch, _lib, L, O = env
+    from sfft_gb300 import signals
+    sigs = [(n, k, V2, FP32) for n, k in _uneven_shapes(10, seed0=70)]
+    xs = [signals.make_signal_torch(n, k, 500 + i, snr_db=40.0)[0].to(torch.complex64)
+          for i, (n, k, _, _) in enumerate(sigs)]
+    torch.cuda.synchronize()
+    mg = _create_tuned(L, _lib, sigs, False, in_type=1)
+    mp = _create_tuned(L, _lib, sigs, True, in_type=1)
+    seeds = [9 + i for i in range(len(sigs))]
+    _run(L, _lib, mg, xs, seeds)
+    _run(L, _lib, mp, xs, seeds)
+    for s in range(len(sigs)):
+        gi, gv = _result(torch, _lib, L, mg, s)
+        pi, pv = _result(torch, _lib, L, mp, s)
+        np.testing.assert_array_equal(pi, gi)
+        np.testing.assert_array_equal(pv, gv)
+    L.sfft_mixed_destroy(mg)
+    L.sfft_mixed_destroy(mp)

@@ -96,10 +96,11 @@ def test_noalloc_alternating_plans_of_different_sizes(env):
     from sfft_gb300 import signals
     from sfft_gb300.sfft import sfft
     shapes = [(1 << 16, 50, 1, "fp64"), (1 << 17, 64, 1, "fp32"), (1 << 18, 50, 2, "fp64"),
-              (1 << 16, 50, 2, "fp32"), (1 << 18, 100, 1, "fp64"), (1 << 17, 64, 2, "fp64")]
+              (1 << 16, 50, 2, "fp32"), (1 << 18, 100, 1, "fp64"), (1 << 17, 64, 2, "fp64"),
+              (1 << 17, 64, 2, "fp32")]     # FP32 v2 estimated by comb residue class
     plans = [sfft(n, k, v, precision=p) for n, k, v, p in shapes]
     stream = torch.cuda.Stream()
-    order = [0, 1, 2, 0, 3, 4, 1, 0, 5, 2, 4, 0, 3, 1, 5, 4, 0, 2, 1, 0]   # large after small and back
+    order = [0, 1, 2, 0, 3, 4, 1, 6, 0, 5, 2, 4, 6, 0, 3, 1, 5, 4, 0, 2, 6, 1, 0]   # large after small and back
     for call, i in enumerate(order):
         n, k, v, p = shapes[i]
         seed = 300 + call
