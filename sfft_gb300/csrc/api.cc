@@ -190,13 +190,12 @@ namespace {
 int L12(const PlanImpl &P) { return P.p12.loops_loc + P.p12.loops_est; }
 
 // Bucket layout of a v1/v2 plan's x_samp (V12Dev::xs_perm): grouped by comb
-// residue for plain FP32 v2 whose comb width W is a multiple of both n / B
-// and that has at least 32 candidates per residue; natural (0) otherwise.
-// (The FP64 form keeps the natural layout: its estimation is bound by the
-// exact FP64 divisions, not by the bucket lookups.)
+// residue for plain v2 (FP32 or FP64) whose comb width W is a multiple of
+// both n / B and that has at least 32 candidates per residue; natural (0)
+// otherwise.
 int xs_perm_of(const PlanImpl &P) {
   const auto &p = P.p12;
-  if (P.version != 1 || P.voted || P.large_b || P.prec != sfft::PREC_FP32 || p.W_Comb <= 0) return 0;
+  if (P.version != 1 || P.voted || P.large_b || p.W_Comb <= 0) return 0;
   const long ql = P.n / p.B_loc, qe = P.n / p.B_est, R = P.n / p.W_Comb;
   if (p.W_Comb % ql || p.W_Comb % qe || R < 32) return 0;
   return ilog2(std::min<long>(R, 256));

@@ -1061,15 +1061,20 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
                : "memory");
 }
 
-// Candidates [h0, h0 + NTH) of a slot (h0 < total, the slot's candidate
-// count; total is a multiple of G, so a group is wholly live or wholly past
-// the end).  Every thread of a block of NTH threads calls it; seg holds
-// L * NTH float2.  The mbarrier in sh is initialised here; a caller that
-// runs another item with the same sh invalidates it first, after a block
-// barrier.
-template <int LN, bool EXACT, int NTH>
-__device__ __forceinline__ void ec32_block(const V12Dev &d, int slot, long h0, long total, float2 *seg,
-                                           EcShared<NTH> &sh) {
+// Staging of candidates [h0, h0 + NTH) of a slot (h0 < total, the slot's
+// candidate count; total is a multiple of G, so a group is wholly live or
+// wholly past the end): one thread per (group, loop) writes the group's
+// table entry for that loop and issues one bulk copy of the group's run of
+// FP32 bucket values (xsrc) into seg (L * NTH float2); then every thread
+// waits.  Every thread of a block of NTH threads calls it.  The mbarrier in
+// sh is initialised here; a caller that stages another item with the same
+// sh invalidates it first, after a block barrier.  srcmw (optional)
+// receives each (group, loop)'s run start and window index.  Returns the
+// live groups, or -1 if the wait timed out.
+template <int NTH>
+__device__ __forceinline__ int ec_stage(const V12Dev &d, int slot, long h0, long total, float2 *seg,
+                                        EcShared<NTH> &sh, const float2 *xsrc, const float2 *wl, const float2 *we,
+                                        int2 *srcmw) {
   const int L = d.L, lg = d.xs_perm, G = 1 << lg, units = NTH >> lg;
   const unsigned R = (unsigned)(d.n / d.W);
   const int live = (int)min((long)units, (total - h0) >> lg);
@@ -1105,20 +1110,31 @@ __device__ __forceinline__ void ec32_block(const V12Dev &d, int slot, long h0, l
     const unsigned beta = (c0 + (unsigned)(d.W / s.q) * (unsigned)grp * ai) & ((unsigned)s.B - 1u);
     const int lt = dlog2((unsigned)s.B) - lg;
     const int src = (int)s.off + (int)((beta & ((1u << lt) - 1u)) << lg);
-    const float2 g = __ldg((const float2 *)(j < d.L_loc ? d.win_loc : d.win_est) + mw);
+    const float2 g = __ldg((j < d.L_loc ? wl : we) + mw);
     sh.v[u * L + j] = EcVal{(int)(beta >> lt), ai, g.x, g.y};
-    bulk_load(seg + j * NTH + (u << lg), (const float2 *)d.xs + (long)slot * d.xs_size + src,
-              (unsigned)(G * sizeof(float2)), &sh.bar);
+    if (srcmw) srcmw[u * L + j] = make_int2(src, mw);
+    // the buffer's previous contents were read through the generic proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    bulk_load(seg + j * NTH + (u << lg), xsrc + (long)slot * d.xs_size + src, (unsigned)(G * sizeof(float2)),
+              &sh.bar);
     mbar_arrive(&sh.bar);
   }
-  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
   // every thread waits (bounded) on its own
   if (!mbar_wait_bounded(&sh.bar, 0)) {
     atomicOr(&d.counters[slot * CNT_STRIDE + CNT_ERR], ERR_WAIT_TIMEOUT);
     mbar_wait_bounded(&sh.bar, 0);  // copies still in flight land before the block moves on
-    return;
+    return -1;
   }
-  if (u >= live) return;
+  return live;
+}
+
+// FP32 estimates of a staged item's live groups (see ec_stage).
+template <int LN, bool EXACT, int NTH>
+__device__ __forceinline__ void ec32_compute(const V12Dev &d, int slot, long h0, int live, const float2 *seg,
+                                             const EcShared<NTH> &sh) {
+  const int L = d.L, lg = d.xs_perm, G = 1 << lg;
+  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
+  if (u >= live) return;  // also after a timeout (live < 0)
   const int Lr = EXACT ? LN : L;
   const EcVal *tv = sh.v + u * L;
   const float2 *sg = seg + (u << lg);
@@ -1136,10 +1152,120 @@ __device__ __forceinline__ void ec32_block(const V12Dev &d, int slot, long h0, l
     }
   }
   const float mre = lower_median<LN, EXACT>(re, Lr), mim = lower_median<LN, EXACT>(im, Lr);
-  const unsigned S = R >> lg;
+  const unsigned S = (unsigned)(d.n / d.W) >> lg;
   const long o = (long)slot * d.out_stride + h0 + threadIdx.x;
   d.out_idx[o] = (int)(((unsigned)sh.grp[u] + S * (unsigned)i) * (unsigned)d.W + (unsigned)sh.res[u]);
   ((float2 *)d.out_val)[o] = make_float2(mre, mim);
+}
+
+// One item staged, waited for and estimated in FP32.
+template <int LN, bool EXACT, int NTH>
+__device__ __forceinline__ void ec32_block(const V12Dev &d, int slot, long h0, long total, float2 *seg,
+                                           EcShared<NTH> &sh) {
+  const int live = ec_stage<NTH>(d, slot, h0, total, seg, sh, (const float2 *)d.xs, (const float2 *)d.win_loc,
+                                 (const float2 *)d.win_est, nullptr);
+  ec32_compute<LN, EXACT, NTH>(d, slot, h0, live, seg, sh);
+}
+
+// Exact FP64 value of loop j of a staged candidate: the reference's
+// operation sequence on the FP64 bucket value and window.
+__device__ __forceinline__ double2 ec_exact64(const V12Dev &d, const EcVal &t, int2 sm, const double2 *xs, int i,
+                                             int G, int j) {
+  const int idx = (int)(((unsigned)t.rot + (unsigned)i * t.ai) & (unsigned)(G - 1));
+  const double2 x = xs[sm.x + idx];
+  const double2 *wp = (const double2 *)(j < d.L_loc ? d.win_loc : d.win_est) + 2 * sm.y;
+  const double2 hw = __ldg(wp);
+  const double den = __ldg(wp + 1).x;
+  using A = Ar<double>;
+  return make_double2(A::div(A::add(A::mul(x.x, hw.x), A::mul(x.y, hw.y)), den),
+                      A::div(A::sub(A::mul(x.x, hw.y), A::mul(x.y, hw.x)), den));
+}
+
+__device__ __noinline__ double2 ec_median64_all(const V12Dev &d, const EcVal *tv, const int2 *sm, const double2 *xs,
+                                                int i, int G) {
+  double vre[EC_MAXL], vim[EC_MAXL];
+  const int L = d.L;
+  for (int j = 0; j < L; j++) {
+    const double2 v = ec_exact64(d, tv[j], sm[j], xs, i, G, j);
+    vre[j] = v.x;
+    vim[j] = v.y;
+  }
+  const int m = (L - 1) >> 1;
+  double mre = 0, mim = 0;
+  for (int a = 0; a < L; a++) {
+    const long long ka = okey(vre[a]), kb = okey(vim[a]);
+    int rr = 0, ri = 0;
+    for (int b = 0; b < L; b++) {
+      const long long x = okey(vre[b]), y = okey(vim[b]);
+      rr += (x < ka) || (b < a && x == ka);
+      ri += (y < kb) || (b < a && y == kb);
+    }
+    if (rr == m) mre = vre[a];
+    if (ri == m) mim = vim[a];
+  }
+  return make_double2(mre, mim);
+}
+
+// FP64 estimates of the staged candidates, bit-exact: the lower-median
+// element of each component is chosen on the staged FP32 copy and proven
+// with the bound of k_estimate64 (proven_median), then divided exactly in
+// FP64; anything not provable takes the all-exact path.
+template <int LN, bool EXACT, int NTH>
+__device__ __forceinline__ void ec64_block(const V12Dev &d, int slot, long h0, long total, float2 *seg,
+                                           EcShared<NTH> &sh, int2 *srcmw) {
+  const int live = ec_stage<NTH>(d, slot, h0, total, seg, sh, (const float2 *)d.xs32,
+                                 (const float2 *)d.win32_loc, (const float2 *)d.win32_est, srcmw);
+  const int L = d.L, lg = d.xs_perm, G = 1 << lg;
+  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
+  if (u >= live) return;
+  const int Lr = EXACT ? LN : L;
+  const EcVal *tv = sh.v + u * L;
+  const int2 *sm = srcmw + u * L;
+  const float2 *sg = seg + (u << lg);
+  const double2 *xs = (const double2 *)d.xs + (long)slot * d.xs_size;
+  // One component at a time (fewer live registers, more resident warps):
+  // the real part's values and bounds, its proven median, whose exact FP64
+  // value is then computed (unconditionally, at a valid index, so that its
+  // loads and divisions overlap the imaginary part's selection); then the
+  // imaginary part's values with the same bounds.
+  float v[LN], eb[LN];
+#pragma unroll
+  for (int j = 0; j < LN; j++) {
+    if (EXACT || j < Lr) {
+      const EcVal t = tv[j];
+      const float2 x = sg[j * NTH + (int)(((unsigned)t.rot + (unsigned)i * t.ai) & (unsigned)(G - 1))];
+      v[j] = x.x * t.gx + x.y * t.gy;
+      // the bound of k_estimate64: |exact - approx| <= 2^-22 (|a| + |b|)(|g.x| + |g.y|), with a 4x margin
+      eb[j] = (fabsf(x.x) + fabsf(x.y)) * (fabsf(t.gx) + fabsf(t.gy)) * 0x1p-20f + 1e-30f;
+    } else {
+      v[j] = INFINITY;
+      eb[j] = 0.f;
+    }
+  }
+  const int ir = proven_median<LN, EXACT>(v, eb, Lr);
+  const int jr = max(ir, 0);
+  const double xre = ec_exact64(d, tv[jr], sm[jr], xs, i, G, jr).x;
+#pragma unroll
+  for (int j = 0; j < LN; j++) {
+    if (EXACT || j < Lr) {
+      const EcVal t = tv[j];
+      const float2 x = sg[j * NTH + (int)(((unsigned)t.rot + (unsigned)i * t.ai) & (unsigned)(G - 1))];
+      v[j] = x.x * t.gy - x.y * t.gx;
+    }
+  }
+  const int ii = proven_median<LN, EXACT>(v, eb, Lr);
+  double2 res;
+  if (ir >= 0 && ii >= 0) {
+    res.x = xre;
+    res.y = ec_exact64(d, tv[ii], sm[ii], xs, i, G, ii).y;
+  } else {
+    res = ec_median64_all(d, tv, sm, xs, i, G);
+    atomicAdd(&d.counters[slot * CNT_STRIDE + CNT_EXACT], 1);
+  }
+  const unsigned S = (unsigned)(d.n / d.W) >> lg;
+  const long o = (long)slot * d.out_stride + h0 + threadIdx.x;
+  d.out_idx[o] = (int)(((unsigned)sh.grp[u] + S * (unsigned)i) * (unsigned)d.W + (unsigned)sh.res[u]);
+  ((double2 *)d.out_val)[o] = res;
 }
 
 __device__ __forceinline__ long ec_total(const V12Dev &d, int slot) {
@@ -1155,6 +1281,18 @@ __global__ void __launch_bounds__(EC_THREADS, 4) k_estimate_comb32(V12Dev d) {
   const long total = ec_total(d, slot), h0 = (long)blockIdx.x * EC_THREADS;
   if (h0 >= total) return;
   ec32_block<LN, EXACT, EC_THREADS>(d, slot, h0, total, seg, sh);
+}
+
+template <int LN, bool EXACT>
+__global__ void __launch_bounds__(EC_THREADS, 3) k_estimate_comb64(V12Dev d) {
+  extern __shared__ __align__(128) float2 seg64[];   // [loop][EC_THREADS]
+  __shared__ EcShared<EC_THREADS> sh;
+  __shared__ int2 srcmw[(EC_THREADS / 32) * EC_MAXL];
+  const int slot = blockIdx.y;
+  if (blockIdx.x == 0 && threadIdx.x == 0) publish_count(d, slot, cand_total(d, slot));
+  const long total = ec_total(d, slot), h0 = (long)blockIdx.x * EC_THREADS;
+  if (h0 >= total) return;
+  ec64_block<LN, EXACT, EC_THREADS>(d, slot, h0, total, seg64, sh, srcmw);
 }
 
 // ---------------------------------------------------------------- scatter --
@@ -1295,9 +1433,24 @@ struct EcK32 {
   }
 };
 
+template <int LN, bool EX>
+struct EcK64 {
+  static cudaError_t go(int nslots, cudaStream_t s, const V12Dev &d, int) {
+    const long cmax = std::min<long>(d.W, (long)d.comb_loops * d.num);
+    const long cands = std::min<long>(cmax * (d.n / d.W), (long)d.out_cap);
+    const size_t sm = sizeof(float2) * EC_THREADS * d.L;
+    cudaError_t e;
+    if ((e = set_smem(k_estimate_comb64<LN, EX>, sm))) return e;
+    dim3 g((unsigned)((cands + EC_THREADS - 1) / EC_THREADS), nslots);
+    k_estimate_comb64<LN, EX><<<g, EC_THREADS, sm, s>>>(d);
+    return cudaSuccess;
+  }
+};
+
 template <typename R>
 static cudaError_t launch_estimate(const V12Dev &d, int nslots, cudaStream_t s) {
   if (sizeof(R) == 4 && d.xs_perm) return dispatch_estimate<EcK32>(d, nslots, 0, s);
+  if (sizeof(R) == 8 && d.xs_perm) return dispatch_estimate<EcK64>(d, nslots, 0, s);
   if (sizeof(R) == 8) return dispatch_estimate<k_estimate64_k>(d, nslots, sm_count(), s);
   return dispatch_estimate<k_estimate32_k>(d, nslots, sm_count(), s);
 }
