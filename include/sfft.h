@@ -181,7 +181,8 @@ int sfft_sync(sfft_plan *plan);
  * precision); 4 v2 comb residues (int, count returned); 5 v3 rounds;
  * 6 v3 estimates as (round, stage, frequency, re, im) doubles;
  * 7 the 16 counters of slot 0 (0 hits, 1 comb residues, 2 outputs, 3 error
- * bits, 4 voted, 8 FP64 medians that took the all-exact path); 8 / 9 the
+ * bits, 4 frequencies that reached the vote threshold (v1 and voted v2),
+ * 8 FP64 medians that took the all-exact path); 8 / 9 the
  * v1/v2 estimation window of the location / estimation filter as held on
  * the device (FP64 plans: n/B entries of (c, d, c^2 + d^2, 0) doubles, the
  * filter.freq values estimate_values divides by; FP32 plans: n/B

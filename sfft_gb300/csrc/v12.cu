@@ -244,10 +244,18 @@ __global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) { comb_list_block(
 // (epoch << 8) resets a counter of an earlier execution to zero votes and
 // leaves one of this execution alone; the atomic add that follows (same
 // address, same thread: ordered after it) returns this vote's count.  One
-// round trip, no compare-and-swap loop.
+// round trip, no compare-and-swap loop.  Plain v2 builds no hit list from
+// its votes -- every frequency they reach is a comb candidate, all of
+// which are estimated (computefourier-1.0-2.0.cc:505-512) -- so its votes
+// only count: both atomics are reductions without a returned value, and
+// the voting threads do not wait for them.
 __device__ __forceinline__ void vote_one(const V12Dev &d, int slot, unsigned f, unsigned ep, unsigned *score,
                                          int *cnt) {
   atomicMax(&score[f], ep << 8);
+  if (d.version == 1 && !d.voted) {
+    atomicAdd(&score[f], 1u);
+    return;
+  }
   const unsigned nv = atomicAdd(&score[f], 1u) + 1u;
   if ((int)(nv & 255u) == d.thresh) {
     atomicAdd(&cnt[CNT_VOTED], 1);
