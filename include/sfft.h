@@ -190,6 +190,15 @@ int sfft_sync(sfft_plan *plan);
  * Returns the number of elements written, or -1. */
 long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap);
 
+/* The selection network the estimators use for the lower median of n
+ * values (n = 8..24, the loop counts whose networks are compiled): writes
+ * (i, j, kind) per comparator in execution order -- kind 1 sets v[i] =
+ * min, v[j] = max; 2 only v[i] = min(v[i], v[j]); 3 only v[j] =
+ * max(v[i], v[j]) -- after which v[(n - 1) / 2] is the lower median.
+ * Host only; returns the comparator count, or -1 (unsupported n, or cap
+ * below 3 ints per comparator). */
+int sfft_debug_median_network(int n, int *dst, long cap);
+
 /* Stage timing with CUDA events recorded on the launching stream.
  * sfft_profile(plan, 1) starts (and zeroes) it; sfft_profile_read waits for
  * the recorded launches and writes the summed milliseconds per stage

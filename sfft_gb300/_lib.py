@@ -87,6 +87,8 @@ def load(build_if_missing=False):
     L.sfft_sync.argtypes = [PP]
     L.sfft_debug_fetch.restype = cl
     L.sfft_debug_fetch.argtypes = [PP, ci, vp, cl]
+    L.sfft_debug_median_network.restype = ci
+    L.sfft_debug_median_network.argtypes = [ci, vp, cl]
     L.sfft_describe_plan.restype = ci
     L.sfft_describe_plan.argtypes = [ci, ci, ci, ctypes.POINTER(cl), ci]
     L.sfft_describe_filter.restype = ci

@@ -93,3 +93,46 @@ def test_tuned_constants_lookup(lib):
                 assert B >= 2 * k + 1
                 assert 1 <= p.threshold_loops <= p.loc_loops and p.est_loops >= 1
     assert lib.sfft_tuned_params(1 << 16, 10, 2, ctypes.byref(_lib.Params())) == -1   # v3: none
+
+
+def _median_network(lib, n):
+    buf = np.zeros(3 * 512, dtype=np.int32)
+    c = lib.sfft_debug_median_network(n, buf.ctypes.data, buf.size)
+    assert c > 0
+    return buf[:3 * c].reshape(c, 3)
+
+
+@pytest.mark.parametrize("n", list(range(8, 25)))
+def test_median_networks_exhaustive(lib, n):
+    """Every compiled lower-median selection network, on all 2^n inputs of
+    0s and 1s: a network of min/max operations selects the m-th smallest
+    of any n values iff it does so for every 0-1 input (min and max commute
+    with monotone maps).  Element (n-1)/2 of the output must be 1 exactly
+    when at least n - (n-1)/2 inputs are 1."""
+    net = _median_network(lib, n)
+    m = (n - 1) // 2
+    chunk = 1 << min(n, 20)
+    for base in range(0, 1 << n, chunk):
+        x = np.arange(base, base + chunk, dtype=np.uint32)
+        v = [((x >> np.uint32(w)) & np.uint32(1)).astype(bool) for w in range(n)]
+        ones = np.zeros(chunk, dtype=np.int32)
+        for w in range(n):
+            ones += v[w]
+        for i, j, kind in net:
+            if kind == 1:
+                v[i], v[j] = v[i] & v[j], v[i] | v[j]
+            elif kind == 2:
+                v[i] = v[i] & v[j]
+            else:
+                assert kind == 3
+                v[j] = v[i] | v[j]
+        np.testing.assert_array_equal(v[m], ones >= n - m)
+
+
+def test_median_network_sizes(lib):
+    """The pruned pairwise networks: fewer min/max operations than the
+    pruned merge-exchange networks they replaced (143 for n = 20)."""
+    ops = {n: int(sum(2 if k == 1 else 1 for _, _, k in _median_network(lib, n))) for n in (8, 12, 16, 20, 24)}
+    assert ops[20] == 125, ops
+    assert ops == {8: 27, 12: 53, 16: 87, 20: 125, 24: 169}, ops
+    assert lib.sfft_debug_median_network(7, None, 0) == -1
