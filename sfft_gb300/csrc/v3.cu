@@ -5,9 +5,9 @@
 //                 contiguous Gaussian fold (:130-212) and of the permuted
 //                 Gaussian fold (:215-297), each followed by its
 //                 shared-memory FFT.  The permuted samples of the second
-//                 fold use the reference's running phase product (:66-87),
-//                 replayed on one thread so its rounding matches, then
-//                 applied to the gathered samples by every thread.
+//                 fold take the phases of the reference's running product
+//                 (:66-87), formed in double-double from tables of its
+//                 factor's powers, one sample per thread.
 //   k_v3_peel     one thread-block cluster (8 CTAs) per signal runs
 //                 alternate_fft's estimate / peel rounds (:784-1088):
 //                 bucket estimation spread over the cluster, subtraction of
@@ -34,6 +34,64 @@ __device__ __forceinline__ double2 ld_x(const void *base, int in_type, long i) {
 }
 
 // --------------------------------------------------------------- filters --
+
+// Double-double numbers (hi + lo, |lo| <= ulp(hi) / 2) with the error-free
+// transformations of Knuth (TwoSum) and of Dekker with a fused
+// multiply-add (TwoProduct): sums and products to about 2^-104 relative.
+struct DD {
+  double hi, lo;
+};
+struct CDD {
+  DD re, im;
+};
+
+__device__ __forceinline__ DD dd_quick(double a, double b) {  // |a| >= |b|
+  const double s = __dadd_rn(a, b);
+  return DD{s, __dsub_rn(b, __dsub_rn(s, a))};
+}
+
+__device__ __forceinline__ DD dd_add(DD x, DD y) {
+  const double s = __dadd_rn(x.hi, y.hi);
+  const double bb = __dsub_rn(s, x.hi);
+  const double e = __dadd_rn(__dsub_rn(x.hi, __dsub_rn(s, bb)), __dsub_rn(y.hi, bb));
+  return dd_quick(s, __dadd_rn(e, __dadd_rn(x.lo, y.lo)));
+}
+
+__device__ __forceinline__ DD dd_neg(DD x) { return DD{-x.hi, -x.lo}; }
+
+__device__ __forceinline__ DD dd_mul(DD x, DD y) {
+  const double p = __dmul_rn(x.hi, y.hi);
+  const double e = __fma_rn(x.hi, y.hi, -p);
+  return dd_quick(p, __fma_rn(x.hi, y.lo, __fma_rn(x.lo, y.hi, e)));
+}
+
+__device__ __forceinline__ CDD cdd(double re, double im) { return CDD{DD{re, 0.0}, DD{im, 0.0}}; }
+
+__device__ __forceinline__ CDD cdd_mul(CDD a, CDD b) {
+  return CDD{dd_add(dd_mul(a.re, b.re), dd_neg(dd_mul(a.im, b.im))), dd_add(dd_mul(a.re, b.im), dd_mul(a.im, b.re))};
+}
+
+// Split of the permuted Gaussian fold's phase products into tables:
+// LO = the power of two at or above sqrt(count) entries of step^lo and
+// ceil(count / LO) of shift_0 step^(LO hi), 32 bytes each, in the filter
+// kernel's shared memory.
+__host__ __device__ __forceinline__ int v3_phase_lo(int count) {
+  int lo = 1;
+  while ((long)lo * lo < count) lo *= 2;
+  return lo;
+}
+
+// a^e, e >= 0, by binary powering.
+__device__ __forceinline__ CDD cdd_pow(CDD a, int e) {
+  CDD r = cdd(1.0, 0.0);
+  while (e) {
+    if (e & 1) r = cdd_mul(r, a);
+    e >>= 1;
+    if (e) a = cdd_mul(a, a);
+  }
+  return r;
+}
+
 
 template <int PER>
 __global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d, int role0) {
@@ -79,26 +137,38 @@ __global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d, int role0) {
     const double2 *taps = (const double2 *)d.taps2;
     // permute_fourier (computefourier-3.0.cc:66-87): sample i is
     // x[(ig + i*ai) mod n] * shift_i with shift_0 = e^{2 pi i ig b / n} and
-    // shift_{i+1} = shift_i * e^{2 pi i ai b / n}, a running product whose
-    // rounding is part of the reference's result.  The product is a serial
-    // chain of rounded complex multiplications: one thread replays it into
-    // P (no memory load on the chain), then every thread multiplies its
-    // samples by their shifts.
+    // shift_{i+1} = shift_i * e^{2 pi i ai b / n}, a running product.  Its
+    // two factors are formed here as there (the same FP64 angles, cos and
+    // sin), but the product is not replayed serially: on GB300's FP64 pipe a
+    // one-thread chain of rounded complex multiplications costs about 64
+    // cycles per operation (2945 steps at n = 2^24, k = 1000: 0.58 ms).
+    // Every thread instead forms shift_i = shift_0 * step^i in double-double
+    // arithmetic from two tables -- step^lo for lo < LO and shift_0 *
+    // step^(LO hi) -- built by binary powering, and rounds it to FP64.  It
+    // differs from the serial chain by that chain's own accumulated rounding
+    // (about i * 2^-53 relative), which is far inside the 1e-10 value
+    // tolerance against the reference.
     double2 *P = (double2 *)d.perm + (long)slot * (d.w2 + 2) * 2 + (long)l * (d.w2 + 2);
     const int count = chunks * N + 1;
-    if (threadIdx.x == 0) {
+    const int LO = v3_phase_lo(count), HI = (count + LO - 1) / LO;
+    CDD *tab = (CDD *)smem_raw;  // [LO] step^lo, then [HI] shift_0 step^(LO hi)
+    {
       const double a0 = 2 * kPi * ig * bb / d.n, a1 = 2 * kPi * ai * bb / d.n;
-      double2 sh = make_double2(cos(a0), sin(a0));
-      const double2 st = make_double2(cos(a1), sin(a1));
-      for (int i = 0; i < count; i++) {
-        if (i >= l) P[i - l] = sh;
-        sh = cmul<double>(sh, st);
+      const CDD sh0 = cdd(cos(a0), sin(a0)), st = cdd(cos(a1), sin(a1));
+      for (int e = threadIdx.x; e < LO + HI; e += blockDim.x) {
+        if (e < LO) {
+          tab[e] = cdd_pow(st, e);
+        } else {
+          tab[e] = cdd_mul(sh0, cdd_pow(cdd_pow(st, LO), e - LO));
+        }
       }
     }
     __syncthreads();
     for (int i = l + threadIdx.x; i < count; i += blockDim.x) {
+      const CDD sh = cdd_mul(tab[LO + i / LO], tab[i % LO]);
+      const double2 shift = make_double2(__dadd_rn(sh.re.hi, sh.re.lo), __dadd_rn(sh.im.hi, sh.im.lo));
       const long index = (long)(((unsigned long long)ig + (unsigned long long)i * (unsigned)ai) % (unsigned)d.n);
-      P[i - l] = cmul<double>(ld_x(x, d.in_type, index), P[i - l]);
+      P[i - l] = cmul<double>(ld_x(x, d.in_type, index), shift);
     }
     __syncthreads();
     for (int b = threadIdx.x; b < N; b += blockDim.x) {
@@ -533,7 +603,8 @@ cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t s, StageEvents *se) 
   if (T > 1024) T = 1024;
   if (T < 32) T = 32;
   const int per = (Nmax / 4 + T - 1) / T;
-  const size_t sm = (size_t)Nmax * sizeof(double2);
+  const int count2 = (d.w2 / d.B2) * d.B2 + 1, lo2 = v3_phase_lo(count2);
+  const size_t sm = std::max((size_t)Nmax * sizeof(double2), sizeof(CDD) * (size_t)(lo2 + (count2 + lo2 - 1) / lo2));
   mark(se, s);
   int role0 = 0;
   if (d.large_man) {
