@@ -940,10 +940,10 @@ def roofline(p32, st32, B):
                            "3.4x the algorithmic bytes (58.8 MB per signal at 73% of peak DRAM throughput in "
                            "ncu); one read of the signal (9.4 us) is the floor, the kernel takes ~10 us")
     out["estimate"]["note"] = ("bound by the ALU pipe, not HBM: the two lower-median selection networks "
-                               "(FMNMX) keep it at 61% of peak in ncu (profiles/k_estimate_comb32_*); every "
-                               "staged bucket byte is read once (56 MB of L2 reads per signal); its HBM bytes "
-                               "are the sparse output")
-    out["estimate"]["alu_pipe_pct_ncu"] = 60.8
+                               "(FMNMX, 2 x 125 per candidate) keep it at 59% of peak in ncu "
+                               "(profiles/k_estimate_comb32_*); every staged bucket byte is read once (58 MB of L2 "
+                               "reads per signal); its HBM bytes are the sparse output")
+    out["estimate"]["alu_pipe_pct_ncu"] = 59.2
     dominant = max(per, key=per.get) if per else "estimate"
     roof = dict(out.get(dominant, out["estimate"]))
     roof["stage"] = dominant

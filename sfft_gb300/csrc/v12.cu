@@ -1173,16 +1173,15 @@ __device__ __forceinline__ int ec_stage(const V12Dev &d, int slot, long h0, long
   const int L = d.L, lg = d.xs_perm, G = 1 << lg, units = NTH >> lg;
   const unsigned R = (unsigned)(d.n / d.W);
   const int live = (int)min((long)units, (total - h0) >> lg);
-  // the barrier completes once the byte count is announced, every (group,
-  // loop) thread has written its table entry and issued its copy (release),
-  // and all copied bytes have landed
-  if (threadIdx.x == 0) {
-    mbar_init(&sh.bar, 1 + live * L);
-    mbar_expect(&sh.bar, (unsigned)(live * L * G * sizeof(float2)));
-  }
-  __syncthreads();
-  if (threadIdx.x < live * L) {
-    const int u = threadIdx.x / L, j = threadIdx.x - u * L;
+  // One thread per (group, loop): its loads and index arithmetic first, so
+  // that they overlap the barrier's initialisation.
+  const bool tab = threadIdx.x < live * L;
+  int j = 0, u = 0, src = 0, mw = 0, rot = 0;
+  unsigned ai = 0;
+  float2 g = make_float2(0.f, 0.f);
+  if (tab) {
+    u = threadIdx.x / L;
+    j = threadIdx.x - u * L;
     const long h = h0 + ((long)u << lg);
     const int ridx = (int)(h / R);
     const int res = d.comb_list[(long)slot * d.W + ridx];
@@ -1193,7 +1192,8 @@ __device__ __forceinline__ int ec_stage(const V12Dev &d, int slot, long h0, long
     }
     const int *rp = d.rparams + (long)slot * d.rp_stride;
     const Slot s = loop_slot(d, j);
-    const unsigned ai = (unsigned)rp[L + j], mask = (unsigned)d.n - 1u;
+    const unsigned mask = (unsigned)d.n - 1u;
+    ai = (unsigned)rp[L + j];
     const unsigned p0 = ((unsigned)res * ai) & mask;
     unsigned c0 = p0 >> s.lq;
     int dist = (int)(p0 & (unsigned)(s.q - 1));
@@ -1201,17 +1201,30 @@ __device__ __forceinline__ int ec_stage(const V12Dev &d, int slot, long h0, long
       c0++;
       dist -= s.q;
     }
-    const int mw = dist + ((s.q - 1) >> 1);
+    mw = dist + ((s.q - 1) >> 1);
     const unsigned beta = (c0 + (unsigned)(d.W / s.q) * (unsigned)grp * ai) & ((unsigned)s.B - 1u);
     const int lt = dlog2((unsigned)s.B) - lg;
-    const int src = (int)s.off + (int)((beta & ((1u << lt) - 1u)) << lg);
-    const float2 g = __ldg((j < d.L_loc ? wl : we) + mw);
-    sh.v[u * L + j] = EcVal{(int)(beta >> lt), ai, g.x, g.y};
-    if (srcmw) srcmw[u * L + j] = make_int2(src, mw);
-    // the buffer's previous contents were read through the generic proxy
+    src = (int)s.off + (int)((beta & ((1u << lt) - 1u)) << lg);
+    rot = (int)(beta >> lt);
+    g = __ldg((j < d.L_loc ? wl : we) + mw);
+  }
+  // the barrier completes once the byte count is announced, every (group,
+  // loop) thread has written its table entry and issued its copy (release),
+  // and all copied bytes have landed
+  if (threadIdx.x == 0) {
+    mbar_init(&sh.bar, 1 + live * L);
+    mbar_expect(&sh.bar, (unsigned)(live * L * G * sizeof(float2)));
+  }
+  __syncthreads();
+  if (tab) {
+    // the copy is issued before the window value is used, so the two loads
+    // overlap (the buffer's previous contents were read through the generic
+    // proxy)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     bulk_load(seg + j * NTH + (u << lg), xsrc + (long)slot * d.xs_size + src, (unsigned)(G * sizeof(float2)),
               &sh.bar);
+    sh.v[u * L + j] = EcVal{rot, ai, g.x, g.y};
+    if (srcmw) srcmw[u * L + j] = make_int2(src, mw);
     mbar_arrive(&sh.bar);
   }
   // every thread waits (bounded) on its own
@@ -1223,17 +1236,15 @@ __device__ __forceinline__ int ec_stage(const V12Dev &d, int slot, long h0, long
   return live;
 }
 
-// FP32 estimates of a staged item's live groups (see ec_stage).
+// The L FP32 values of candidate i of staged group u (see ec_stage):
+// x_samp[bucket] / filter.freq[dist] with the reference's sign.
 template <int LN, bool EXACT, int NTH>
-__device__ __forceinline__ void ec32_compute(const V12Dev &d, int slot, long h0, int live, const float2 *seg,
-                                             const EcShared<NTH> &sh) {
+__device__ __forceinline__ void ec32_values(const V12Dev &d, const float2 *seg, const EcShared<NTH> &sh, int u,
+                                            int i, float (&re)[LN], float (&im)[LN]) {
   const int L = d.L, lg = d.xs_perm, G = 1 << lg;
-  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
-  if (u >= live) return;  // also after a timeout (live < 0)
   const int Lr = EXACT ? LN : L;
   const EcVal *tv = sh.v + u * L;
   const float2 *sg = seg + (u << lg);
-  float re[LN], im[LN];
 #pragma unroll
   for (int j = 0; j < LN; j++) {
     if (EXACT || j < Lr) {
@@ -1246,11 +1257,31 @@ __device__ __forceinline__ void ec32_compute(const V12Dev &d, int slot, long h0,
       im[j] = INFINITY;
     }
   }
+}
+
+// Lower medians of the values and the output entry of candidate i of
+// group (res, grp), position h0 + threadIdx.x of the slot's output.
+template <int LN, bool EXACT>
+__device__ __forceinline__ void ec32_finish(const V12Dev &d, int slot, long h0, int res, int grp, int i,
+                                            float (&re)[LN], float (&im)[LN]) {
+  const int Lr = EXACT ? LN : d.L;
   const float mre = lower_median<LN, EXACT>(re, Lr), mim = lower_median<LN, EXACT>(im, Lr);
-  const unsigned S = (unsigned)(d.n / d.W) >> lg;
+  const unsigned S = (unsigned)(d.n / d.W) >> d.xs_perm;
   const long o = (long)slot * d.out_stride + h0 + threadIdx.x;
-  d.out_idx[o] = (int)(((unsigned)sh.grp[u] + S * (unsigned)i) * (unsigned)d.W + (unsigned)sh.res[u]);
+  d.out_idx[o] = (int)(((unsigned)grp + S * (unsigned)i) * (unsigned)d.W + (unsigned)res);
   ((float2 *)d.out_val)[o] = make_float2(mre, mim);
+}
+
+// FP32 estimates of a staged item's live groups (see ec_stage).
+template <int LN, bool EXACT, int NTH>
+__device__ __forceinline__ void ec32_compute(const V12Dev &d, int slot, long h0, int live, const float2 *seg,
+                                             const EcShared<NTH> &sh) {
+  const int lg = d.xs_perm, G = 1 << lg;
+  const int u = threadIdx.x >> lg, i = threadIdx.x & (G - 1);
+  if (u >= live) return;  // also after a timeout (live < 0)
+  float re[LN], im[LN];
+  ec32_values<LN, EXACT, NTH>(d, seg, sh, u, i, re, im);
+  ec32_finish<LN, EXACT>(d, slot, h0, sh.res[u], sh.grp[u], i, re, im);
 }
 
 // One item staged, waited for and estimated in FP32.
