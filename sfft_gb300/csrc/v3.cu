@@ -236,59 +236,62 @@ __device__ __forceinline__ int wrapmul(int x, int y) { return (int)((unsigned)x 
 // Subtract a recovered tone from the three nearest buckets of both shifts
 // of a Gaussian filter (computefourier-3.0.cc:354-463).
 __device__ void update_gauss(const PeelCtx &c, double2 *SAMP, const double2 *win, int half, int B,
-                             int key, double2 v, int offset, int step, int *err) {
+                             int key, double2 v, int offset, int step, int l, int *err) {
   const int n = c.n, n1 = c.n1;
   const unsigned q = n / B;
-  const int h = (int)(key * 1. / q + 0.5) % B;
+  // key / q with q a power of two: the product with 1 / q is the same double
+  const int h = (int)(key * (1. / q) + 0.5) % B;
   const int dist1 = (int)(((unsigned)h * q - (unsigned)key + (unsigned)n) & (unsigned)n1);
   const int dist2 = (int)(((unsigned)dist1 + (unsigned)n + q) & (unsigned)n1);
   const int dist3 = (int)(((unsigned)dist1 + 2u * (unsigned)n - q) & (unsigned)n1);
-  const int ko1 = wrapmul(key, offset) % n;
-  const int ko2 = wrapmul(key, (int)((unsigned)offset + (unsigned)step)) % n;
+  // shift l of the two: time offset `offset` (l = 0) or `offset + step` (l = 1)
+  const int ko = wrapmul(key, (int)((unsigned)offset + (l ? (unsigned)step : 0u))) % n;
   const double PI2_DIV_N = 2 * kPi / n;
-  double s1, c1, s2, c2;
-  sincos(PI2_DIV_N * ko1, &s1, &c1);
-  sincos(PI2_DIV_N * ko2, &s2, &c2);
-  const double2 v1 = cmul<double>(v, make_double2(c1, s1));
-  const double2 v2 = cmul<double>(v, make_double2(c2, s2));
+  double sn, cs;
+  sincos(PI2_DIV_N * ko, &sn, &cs);
+  const double2 vl = cmul<double>(v, make_double2(cs, sn));
   const int dists[3] = {dist1, dist2, dist3};
   const int bks[3] = {h, (h + 1) % B, (h + B - 1) % B};
 #pragma unroll
   for (int qd = 0; qd < 3; qd++) {
     const double2 f = win_at(win, half, n, dists[qd], err);
-    const double2 r1 = cmul<double>(v1, f), r2 = cmul<double>(v2, f);
-    double *p0 = (double *)&SAMP[2 * bks[qd]];
-    double *p1 = (double *)&SAMP[2 * bks[qd] + 1];
-    atomicAdd(p0, -r1.x);
-    atomicAdd(p0 + 1, -r1.y);
-    atomicAdd(p1, -r2.x);
-    atomicAdd(p1 + 1, -r2.y);
+    const double2 r = cmul<double>(vl, f);
+    double *p = (double *)&SAMP[2 * bks[qd] + l];
+    atomicAdd(p, -r.x);
+    atomicAdd(p + 1, -r.y);
   }
 }
 
-// (computefourier-3.0.cc:300-351)
-__device__ void update_mansour(const PeelCtx &c, int key, double2 v) {
+// (computefourier-3.0.cc:300-351), shift l of the two
+__device__ void update_mansour(const PeelCtx &c, int key, double2 v, int l) {
   const int W = c.d->W;
   const int h = key & (W - 1);
   const double PI2_OVER_N = 2 * kPi / c.n;
-#pragma unroll
-  for (int l = 0; l < 2; l++) {
-    double s, co;
-    sincos(PI2_OVER_N * key * (double)(c.io + l), &s, &co);
-    const double rr = (double)W * (v.x * co - v.y * s);
-    const double ri = (double)W * (v.x * s + v.y * co);
-    double *p = (double *)&c.man[2 * h + l];
-    atomicAdd(p, -rr);
-    atomicAdd(p + 1, -ri);
-  }
+  double s, co;
+  sincos(PI2_OVER_N * key * (double)(c.io + l), &s, &co);
+  const double rr = (double)W * (v.x * co - v.y * s);
+  const double ri = (double)W * (v.x * s + v.y * co);
+  double *p = (double *)&c.man[2 * h + l];
+  atomicAdd(p, -rr);
+  atomicAdd(p + 1, -ri);
 }
 
-__device__ void update_all(const PeelCtx &c, int key, double2 v, int *err) {
+// Subtraction of a recovered tone from one filter's buckets of one shift:
+// part = 2 * filter + shift, filter 0 the permuted Gaussian, 1 the
+// contiguous Gaussian, 2 the Mansour comb.  The six parts of a tone are
+// independent (atomic subtractions), so they are separate work items:
+// their FP64 chains (one sincos each) run on different sub-partitions.
+__device__ void update_part(const PeelCtx &c, int key, double2 v, int part, int *err) {
   const V3Dev &d = *c.d;
-  const int k2 = (int)((((long long)key * c.ai) % c.n + c.shift) % c.n);
-  update_gauss(c, c.g2, (const double2 *)d.win2, d.win2_half, d.B2, k2, v, c.aG, 1, err);
-  update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, key, v, c.ig, 1, err);
-  update_mansour(c, key, v);
+  const int l = part & 1;
+  if (part < 2) {
+    const int k2 = (int)((((long long)key * c.ai) % c.n + c.shift) % c.n);
+    update_gauss(c, c.g2, (const double2 *)d.win2, d.win2_half, d.B2, k2, v, c.aG, 1, l, err);
+  } else if (part < 4) {
+    update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, key, v, c.ig, 1, l, err);
+  } else {
+    update_mansour(c, key, v, l);
+  }
 }
 
 // Result map: key -> accumulated value; returns nothing, keys of one round
@@ -321,77 +324,163 @@ __device__ void map_add(const PeelCtx &c, int key, double2 v, bool assign, int *
   atomicOr(err, ERR_V3_CAP);
 }
 
+// The estimation loops below visit every bucket, but only buckets that pass
+// the reference's zero-bucket check do FP64 work (atan2, sincos, sqrt) --
+// and on GB300 a warp's FP64 instruction occupies its SM sub-partition's
+// narrow FP64 pipe for tens of cycles whether one lane or 32 are active.
+// So each CTA first lists its passing buckets in shared memory (the cheap
+// check), then deals the list out one per lane over warps of all four
+// sub-partitions: the FP64 work of a phase costs about one warp's chain
+// per sub-partition instead of one per warp that holds a passing bucket.
+constexpr int V3_LIST = 1024;  // list entries per CTA and pass (= threads per CTA)
+
+// Position in the list of thread `tid` of a 1024-thread CTA: consecutive
+// entries go to consecutive sub-partitions (warp mod 4), then lanes.
+__device__ __forceinline__ int v3_spread(int tid) {
+  return ((tid >> 7) << 7) | ((tid & 31) << 2) | ((tid >> 5) & 3);
+}
+
+// Per-CTA shared scratch of the estimation loops: the list of passing
+// buckets and, per (entry, shift), the phase and one more quantity.  Each
+// passing bucket is two work items in a first step -- the atan2 of one
+// shift each, plus sqrt(c0) or 1 / c0 -- and one in a second step, so its
+// FP64 chain is split over two sub-partitions.
+struct EstScratch {
+  int list[V3_LIST];
+  int cnt;
+  double ang[2 * V3_LIST], aux[2 * V3_LIST];
+};
+
+// Lists this CTA's buckets among [base + t0] (one per thread) that pass
+// `pass`; every thread of the CTA calls it.  Returns the count.
+__device__ __forceinline__ int est_list(EstScratch &x, int bk, bool pass) {
+  if (threadIdx.x == 0) x.cnt = 0;
+  __syncthreads();
+  if (pass) x.list[atomicAdd(&x.cnt, 1)] = bk;
+  __syncthreads();
+  return x.cnt;
+}
+
 // estimate_freq_mansour_loops2 (computefourier-3.0.cc:642-776)
-__device__ void est_mansour(const PeelCtx &c, int *nfound, int cap, int *err, int t0, int tstride) {
+__device__ void est_mansour(const PeelCtx &c, int *nfound, int cap, int *err, int t0, int tstride, EstScratch &x) {
   const int W = c.d->W, n = c.n;
   const double PI2 = 2 * kPi, N_OVER_PI2 = n / PI2, PI2_OVER_N = PI2 / n;
   const unsigned FREQ_MASK = ((unsigned)(n - 1) & ~((unsigned)W - 1));
   const double NORM = 1. / W, NORM2 = NORM * NORM;
-  for (int bk = t0; bk < W; bk += tstride) {
-    const double2 s0 = c.man[2 * bk], s1 = c.man[2 * bk + 1];
-    const double c0 = (s0.x * s0.x + s0.y * s0.y) * NORM2;
-    const double c1 = (s1.x * s1.x + s1.y * s1.y) * NORM2;
-    if (!(c0 + c1 > 1e-8)) continue;
-    const double d0 = atan2(s0.y * NORM, s0.x * NORM), d1 = atan2(s1.y * NORM, s1.x * NORM);
-    const double bb = (c1 * (1. / c0)) - 1;
-    if ((bb * bb < n * 1e-10) && (c0 > 0.01)) {
-      const int freq1 = (int)__double2ll_rn((d1 - d0) * N_OVER_PI2);
-      const int freq3 = (int)((unsigned)freq1 & FREQ_MASK) | bk;
-      const double ph = d0 - PI2_OVER_N * wrapmul(freq3, c.io);
-      const double ab = sqrt(c0);
-      double s, co;
-      sincos(ph, &s, &co);
-      const int i = atomicAdd(nfound, 1);
-      if (i < cap) {
-        c.est_f[i] = freq3;
-        c.est_v[i] = make_double2(ab * co, ab * s);
-      } else {
-        atomicOr(err, ERR_V3_CAP);
-      }
+  for (int base = 0; base < W; base += tstride) {
+    const int bk0 = base + t0;
+    bool pass = false;
+    if (bk0 < W) {
+      const double2 s0 = c.man[2 * bk0], s1 = c.man[2 * bk0 + 1];
+      const double c0 = (s0.x * s0.x + s0.y * s0.y) * NORM2;
+      const double c1 = (s1.x * s1.x + s1.y * s1.y) * NORM2;
+      pass = c0 + c1 > 1e-8;
     }
-  }
-}
-
-// estimate_freq_gauss_loops2 (computefourier-3.0.cc:484-640)
-__device__ void est_gauss(const PeelCtx &c, const double2 *SAMP, int B, const double2 *win,
-                          int half, int a, int b, int *nfound, int cap, int *err, int t0, int tstride) {
-  const int n = c.n;
-  const unsigned n1 = n - 1, B1 = B - 1;
-  const double PI2 = 2 * kPi, N_OVER_PI2 = n / PI2;
-  const double PI2_A_OFFSET_OVER_N = PI2 * a * c.ig / n;
-  const double BUCKETS_OVER_N = (double)B / n;
-  const unsigned q = n / B;
-  for (int bk = t0; bk < B; bk += tstride) {
-    const double2 s0 = SAMP[2 * bk], s1 = SAMP[2 * bk + 1];
-    const double c0 = s0.x * s0.x + s0.y * s0.y;
-    const double c1 = s1.x * s1.x + s1.y * s1.y;
-    if (!(c0 + c1 > 1e-8)) continue;
-    const double d0 = atan2(s0.y, s0.x), d1 = atan2(s1.y, s1.x);
-    const double eb = c1 / c0 - 1;
-    const double err2 = (eb * eb) / n;
-    if ((err2 < 1e-12) && (c0 > 0.01)) {
-      const int freq = (int)((unsigned)((int)__double2ll_rn(N_OVER_PI2 * (d1 - d0)) + n) & n1);
-      const unsigned hashed = (unsigned)__double2ll_rn(freq * BUCKETS_OVER_N) & B1;
-      if (hashed == (unsigned)bk) {
-        const double ph = d0 - PI2_A_OFFSET_OVER_N * freq;
-        const double r = sqrt(c0);
-        double s, co;
-        sincos(ph, &s, &co);
-        const double mr = r * co, mi = r * s;
-        const int dist = (int)((hashed * q - (unsigned)freq + (unsigned)n) & n1);
-        const double2 f = win_at(win, half, n, dist, err);
-        const double den = f.x * f.x + f.y * f.y;
-        const double2 v = make_double2((mr * f.x + mi * f.y) / den, (mi * f.x - mr * f.y) / den);
-        const int fo = (int)((unsigned)((int)(((long long)freq * a) % n) - b + n) & n1);
+    const int cnt = est_list(x, bk0, pass);
+    for (int w = v3_spread(threadIdx.x); w < 2 * cnt; w += V3_LIST) {
+      const int bk = x.list[w >> 1], l = w & 1;
+      const double2 sl = c.man[2 * bk + l];
+      x.ang[w] = atan2(sl.y * NORM, sl.x * NORM);
+      const double2 s0 = c.man[2 * bk];
+      const double c0 = (s0.x * s0.x + s0.y * s0.y) * NORM2;
+      x.aux[w] = l ? 1. / c0 : sqrt(c0);
+    }
+    __syncthreads();
+    for (int e = v3_spread(threadIdx.x); e < cnt; e += V3_LIST) {
+      const int bk = x.list[e];
+      const double2 s1 = c.man[2 * bk + 1];
+      const double c1 = (s1.x * s1.x + s1.y * s1.y) * NORM2;
+      const double s0x = c.man[2 * bk].x, s0y = c.man[2 * bk].y;
+      const double c0 = (s0x * s0x + s0y * s0y) * NORM2;
+      const double d0 = x.ang[2 * e], d1 = x.ang[2 * e + 1];
+      const double bb = (c1 * x.aux[2 * e + 1]) - 1;
+      if ((bb * bb < n * 1e-10) && (c0 > 0.01)) {
+        const int freq1 = (int)__double2ll_rn((d1 - d0) * N_OVER_PI2);
+        const int freq3 = (int)((unsigned)freq1 & FREQ_MASK) | bk;
+        const double ph = d0 - PI2_OVER_N * wrapmul(freq3, c.io);
+        const double ab = x.aux[2 * e];
+        double sn, co;
+        sincos(ph, &sn, &co);
         const int i = atomicAdd(nfound, 1);
         if (i < cap) {
-          c.est_f[i] = fo;
-          c.est_v[i] = v;
+          c.est_f[i] = freq3;
+          c.est_v[i] = make_double2(ab * co, ab * sn);
         } else {
           atomicOr(err, ERR_V3_CAP);
         }
       }
     }
+    __syncthreads();  // the scratch is reused by the next pass
+  }
+}
+
+// estimate_freq_gauss_loops2 (computefourier-3.0.cc:484-640)
+__device__ void est_gauss(const PeelCtx &c, const double2 *SAMP, int B, const double2 *win,
+                          int half, int a, int b, int *nfound, int cap, int *err, int t0, int tstride,
+                          EstScratch &x) {
+  const int n = c.n;
+  const unsigned n1 = n - 1, B1 = B - 1;
+  const double PI2 = 2 * kPi, N_OVER_PI2 = n / PI2;
+  const double PI2_A_OFFSET_OVER_N = PI2 * a * c.ig / n;
+  const double BUCKETS_OVER_N = (double)B / n;
+  const double INV_N = 1. / n;  // n is a power of two: the product equals the quotient
+  const unsigned q = n / B;
+  for (int base = 0; base < B; base += tstride) {
+    const int bk0 = base + t0;
+    bool pass = false;
+    if (bk0 < B) {
+      const double2 s0 = SAMP[2 * bk0], s1 = SAMP[2 * bk0 + 1];
+      const double c0 = s0.x * s0.x + s0.y * s0.y;
+      const double c1 = s1.x * s1.x + s1.y * s1.y;
+      pass = c0 + c1 > 1e-8;
+    }
+    const int cnt = est_list(x, bk0, pass);
+    for (int w = v3_spread(threadIdx.x); w < 2 * cnt; w += V3_LIST) {
+      const int bk = x.list[w >> 1], l = w & 1;
+      const double2 sl = SAMP[2 * bk + l];
+      x.ang[w] = atan2(sl.y, sl.x);
+      const double2 s0 = SAMP[2 * bk];
+      const double c0 = s0.x * s0.x + s0.y * s0.y;
+      if (l) {
+        const double c1 = sl.x * sl.x + sl.y * sl.y;
+        x.aux[w] = c1 / c0 - 1;
+      } else {
+        x.aux[w] = sqrt(c0);
+      }
+    }
+    __syncthreads();
+    for (int e = v3_spread(threadIdx.x); e < cnt; e += V3_LIST) {
+      const int bk = x.list[e];
+      const double2 s0 = SAMP[2 * bk];
+      const double c0 = s0.x * s0.x + s0.y * s0.y;
+      const double d0 = x.ang[2 * e], d1 = x.ang[2 * e + 1];
+      const double eb = x.aux[2 * e + 1];
+      const double err2 = (eb * eb) * INV_N;
+      if ((err2 < 1e-12) && (c0 > 0.01)) {
+        const int freq = (int)((unsigned)((int)__double2ll_rn(N_OVER_PI2 * (d1 - d0)) + n) & n1);
+        const unsigned hashed = (unsigned)__double2ll_rn(freq * BUCKETS_OVER_N) & B1;
+        if (hashed == (unsigned)bk) {
+          const double ph = d0 - PI2_A_OFFSET_OVER_N * freq;
+          const double r = x.aux[2 * e];
+          double sn, co;
+          sincos(ph, &sn, &co);
+          const double mr = r * co, mi = r * sn;
+          const int dist = (int)((hashed * q - (unsigned)freq + (unsigned)n) & n1);
+          const double2 f = win_at(win, half, n, dist, err);
+          const double den = f.x * f.x + f.y * f.y;
+          const double2 v = make_double2((mr * f.x + mi * f.y) / den, (mi * f.x - mr * f.y) / den);
+          const int fo = (int)((unsigned)((int)(((long long)freq * a) % n) - b + n) & n1);
+          const int i = atomicAdd(nfound, 1);
+          if (i < cap) {
+            c.est_f[i] = fo;
+            c.est_v[i] = v;
+          } else {
+            atomicOr(err, ERR_V3_CAP);
+          }
+        }
+      }
+    }
+    __syncthreads();  // the scratch is reused by the next pass
   }
 }
 
@@ -452,8 +541,13 @@ __global__ void __cluster_dims__(V3_CLUSTER, 1, 1) __launch_bounds__(1024) k_v3_
   c.aG = wrapmul(c.a, c.ig);
   c.shift = ((wrapmul(c.ai, c.b) % d.n) + d.n) % d.n;
   int *cnt = d.counters + slot * CNT_STRIDE;
-  const int T = blockDim.x * V3_CLUSTER;           // the cluster's threads
-  const int gt = rank * blockDim.x + threadIdx.x;  // this thread among them
+  // The cluster's threads; work item i of a loop over the cluster goes to
+  // CTA i mod 8 and, within it, to consecutive sub-partitions and lanes
+  // (v3_spread), so a short loop spreads its FP64 work over all 32
+  // sub-partitions of the cluster's SMs.
+  const int T = blockDim.x * V3_CLUSTER;
+  const int gt = v3_spread(threadIdx.x) * V3_CLUSTER + rank;
+  __shared__ EstScratch est_x;
   const bool lead = rank == 0 && threadIdx.x == 0;
   if (lead) {
     S->found = 0;
@@ -465,7 +559,7 @@ __global__ void __cluster_dims__(V3_CLUSTER, 1, 1) __launch_bounds__(1024) k_v3_
   cl.sync();
 
   // ---- Mansour estimate; first tones are assigned, their buckets cleared
-  est_mansour(c, &S->found, d.est_cap, &S->err, gt, T);
+  est_mansour(c, &S->found, d.est_cap, &S->err, gt, T, est_x);
   cl.sync();
   int F = min(S->found, d.est_cap);
   for (int i = gt; i < F; i += T) {
@@ -488,32 +582,31 @@ __global__ void __cluster_dims__(V3_CLUSTER, 1, 1) __launch_bounds__(1024) k_v3_
 
   // ---- first Gaussian filter: peel the known tones, estimate, peel
   int M = min(S->count, d.map_cap);
-  for (int i = gt; i < M; i += T) {
-    const int h = c.list[i];
-    update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, c.tkey[h], c.tval[h], c.ig, 1,
-                 &S->err);
+  for (int w = gt; w < 2 * M; w += T) {  // items (tone, shift)
+    const int h = c.list[w >> 1];
+    update_part(c, c.tkey[h], c.tval[h], 2 + (w & 1), &S->err);
   }
   if (lead) S->found = 0;
   cl.sync();
-  est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &S->found, d.est_cap, &S->err, gt, T);
+  est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &S->found, d.est_cap, &S->err, gt, T,
+            est_x);
   cl.sync();
   F = min(S->found, d.est_cap);
-  for (int i = gt; i < F; i += T) {
-    trace_rec(d, slot, cnt, -1, 1, c.est_f[i], c.est_v[i]);
-    map_add(c, c.est_f[i], c.est_v[i], false, &S->count, d.map_cap, &S->err);
-    update_gauss(c, c.g1, (const double2 *)d.win1, d.win1_half, d.B1, c.est_f[i], c.est_v[i], c.ig, 1,
-                 &S->err);
-    update_mansour(c, c.est_f[i], c.est_v[i]);
+  for (int w = gt; w < 4 * F; w += T) {  // items (tone, part 2..5)
+    const int i = w >> 2;
+    if (!(w & 3)) {
+      trace_rec(d, slot, cnt, -1, 1, c.est_f[i], c.est_v[i]);
+      map_add(c, c.est_f[i], c.est_v[i], false, &S->count, d.map_cap, &S->err);
+    }
+    update_part(c, c.est_f[i], c.est_v[i], 2 + (w & 3), &S->err);
   }
   cl.sync();
 
   // ---- second (permuted) Gaussian filter: peel every known tone
   M = min(S->count, d.map_cap);
-  for (int i = gt; i < M; i += T) {
-    const int h = c.list[i];
-    const int key = c.tkey[h];
-    const int k2 = (int)((((long long)key * c.ai) % d.n + c.shift) % d.n);
-    update_gauss(c, c.g2, (const double2 *)d.win2, d.win2_half, d.B2, k2, c.tval[h], c.aG, 1, &S->err);
+  for (int w = gt; w < 2 * M; w += T) {  // items (tone, shift)
+    const int h = c.list[w >> 1];
+    update_part(c, c.tkey[h], c.tval[h], w & 1, &S->err);
   }
   cl.sync();
 
@@ -524,18 +617,22 @@ __global__ void __cluster_dims__(V3_CLUSTER, 1, 1) __launch_bounds__(1024) k_v3_
     if (lead) S->found = 0;
     cl.sync();
     if (stage == 0)
-      est_mansour(c, &S->found, d.est_cap, &S->err, gt, T);
+      est_mansour(c, &S->found, d.est_cap, &S->err, gt, T, est_x);
     else if (stage == 1)
-      est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &S->found, d.est_cap, &S->err, gt, T);
+      est_gauss(c, c.g1, d.B1, (const double2 *)d.win1, d.win1_half, 1, 0, &S->found, d.est_cap, &S->err, gt, T,
+                est_x);
     else
       est_gauss(c, c.g2, d.B2, (const double2 *)d.win2, d.win2_half, c.a, c.b, &S->found, d.est_cap, &S->err,
-                gt, T);
+                gt, T, est_x);
     cl.sync();
     F = min(S->found, d.est_cap);
-    for (int i = gt; i < F; i += T) {
-      trace_rec(d, slot, cnt, rounds, stage, c.est_f[i], c.est_v[i]);
-      map_add(c, c.est_f[i], c.est_v[i], false, &S->count, d.map_cap, &S->err);
-      update_all(c, c.est_f[i], c.est_v[i], &S->err);
+    for (int w = gt; w < 6 * F; w += T) {  // items (tone, part)
+      const int i = w / 6, part = w - 6 * i;
+      if (part == 0) {
+        trace_rec(d, slot, cnt, rounds, stage, c.est_f[i], c.est_v[i]);
+        map_add(c, c.est_f[i], c.est_v[i], false, &S->count, d.map_cap, &S->err);
+      }
+      update_part(c, c.est_f[i], c.est_v[i], part, &S->err);
     }
     if (stage == 2 && rounds >= 1 && lead) S->cnt[0] = S->cnt[1] = S->cnt[2] = 0;
     cl.sync();
@@ -549,9 +646,10 @@ __global__ void __cluster_dims__(V3_CLUSTER, 1, 1) __launch_bounds__(1024) k_v3_
         const double2 v = c.g2[j];
         c2 += (v.x * v.x + v.y * v.y > 1e-6);
       }
+      const double inv_w = 1. / d.W;  // W is a power of two: the products equal the quotients
       for (int j = gt; j < d.W; j += T) {
         const double2 v = c.man[2 * j];
-        const double re = v.x / d.W, im = v.y / d.W;
+        const double re = v.x * inv_w, im = v.y * inv_w;
         cm += (re * re + im * im > 1e-6);
       }
       if (cm) atomicAdd(&S->cnt[0], cm);
