@@ -1476,7 +1476,13 @@ long sfft_debug_fetch(sfft_plan *plan, int what, void *dst, long cap) {
         if (!cuda_ok(cudaMemcpy(raw.data(), P->score.p, sizeof(unsigned) * P->n, cudaMemcpyDeviceToHost), "debug"))
           return -1;
         int *o = (int *)dst;
-        for (int i = 0; i < P->n; i++) o[i] = ((raw[i] >> 8) == P->epoch[0]) ? (int)(raw[i] & 255u) : 0;
+        // v2 keeps its counters residue-major: frequency rep W + r at r (n / W) + rep
+        const bool rmaj = P->version == 1;
+        const long W = p.W_Comb, R = rmaj ? P->n / W : 1;
+        for (long i = 0; i < P->n; i++) {
+          const long f = rmaj ? (i % R) * W + i / R : i;
+          o[f] = ((raw[i] >> 8) == P->epoch[0]) ? (int)(raw[i] & 255u) : 0;
+        }
         return P->n;
       }
       case 3: {  // bucket values in natural order

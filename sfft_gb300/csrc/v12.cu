@@ -249,14 +249,23 @@ __global__ void __launch_bounds__(1024) k_comb_list(V12Dev d) { comb_list_block(
 // which are estimated (computefourier-1.0-2.0.cc:505-512) -- so its votes
 // only count: both atomics are reductions without a returned value, and
 // the voting threads do not wait for them.
+// v2's counters are stored residue-major, frequency f = rep W + r at
+// r (n / W) + rep: the votes of a round fall on the few comb residues'
+// blocks of n / W consecutive counters instead of all over the n of them,
+// which keeps the touched counters dense in L2 and DRAM.
 __device__ __forceinline__ void vote_one(const V12Dev &d, int slot, unsigned f, unsigned ep, unsigned *score,
                                          int *cnt) {
-  atomicMax(&score[f], ep << 8);
+  unsigned *c = &score[f];
+  if (d.version == 1) {
+    const int lw = dlog2((unsigned)d.W), lr = dlog2((unsigned)d.n) - lw;
+    c = &score[((f & ((unsigned)d.W - 1u)) << lr) | (f >> lw)];
+  }
+  atomicMax(c, ep << 8);
   if (d.version == 1 && !d.voted) {
-    atomicAdd(&score[f], 1u);
+    atomicAdd(c, 1u);
     return;
   }
-  const unsigned nv = atomicAdd(&score[f], 1u) + 1u;
+  const unsigned nv = atomicAdd(c, 1u) + 1u;
   if ((int)(nv & 255u) == d.thresh) {
     atomicAdd(&cnt[CNT_VOTED], 1);
     if (d.version == 0 || d.voted) {
