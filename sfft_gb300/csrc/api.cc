@@ -130,7 +130,7 @@ struct PlanImpl {
   int slots = 0;
   DBuf xs, xs32, xs_tmp, comb_buf, comb_tmp, J, score, hits, comb_bits, comb_list, counters, out_idx, out_val;
   DBuf man, man_tmp, g1, g2, perm, est_f, est_v, map_keys, map_vals, map_list;
-  DBuf rparams, inputs, dense_ptrs, in_stage, dense_stage, trace;
+  DBuf rparams, inputs, dense_ptrs, in_stage, dense_stage, trace, cnt_stash;
   std::vector<unsigned> epoch;
   int hit_cap = 0, out_cap = 0, est_cap = 0, map_cap = 0, table_cap = 0;
   int large_b = 0, large_c = 0;  // FFTs longer than one CTA's shared memory
@@ -689,12 +689,8 @@ bool launch(PlanImpl &P, int num, const void *const *in_dev, int in_type, cudaSt
   return ok;
 }
 
-bool check_device_errors(PlanImpl &P, int num, int base = 0) {
-  std::vector<int> cnt((size_t)sfft::CNT_STRIDE * num);
-  if (!cuda_ok(cudaMemcpy(cnt.data(), P.counters.as<int>() + (size_t)base * sfft::CNT_STRIDE, sizeof(int) * cnt.size(),
-                          cudaMemcpyDeviceToHost),
-               "counters"))
-    return false;
+// Error bits of `num` signals' counters (CNT_STRIDE ints each, host copy).
+bool check_counts(const int *cnt, int num) {
   for (int i = 0; i < num; i++) {
     const int e = cnt[(size_t)i * sfft::CNT_STRIDE + sfft::CNT_ERR];
     if (e) {
@@ -706,6 +702,15 @@ bool check_device_errors(PlanImpl &P, int num, int base = 0) {
     }
   }
   return true;
+}
+
+bool check_device_errors(PlanImpl &P, int num, int base = 0) {
+  std::vector<int> cnt((size_t)sfft::CNT_STRIDE * num);
+  if (!cuda_ok(cudaMemcpy(cnt.data(), P.counters.as<int>() + (size_t)base * sfft::CNT_STRIDE, sizeof(int) * cnt.size(),
+                          cudaMemcpyDeviceToHost),
+               "counters"))
+    return false;
+  return check_counts(cnt.data(), num);
 }
 
 bool is_device_ptr(const void *p) {
@@ -768,12 +773,17 @@ bool exec_dense_chunk(PlanImpl &P, int num, complex_t **in, complex_t **out) {
 // sfft_exec_many on host buffers: chunk c's input copies (copy_in), its
 // transform (plan stream) and its dense output copies (copy_out) overlap
 // with the neighbouring chunks; workspace, input staging and dense staging
-// are double-buffered (slot halves [0, chunk) and [chunk, 2 chunk)).
+// are double-buffered (slot halves [0, chunk) and [chunk, 2 chunk)).  Each
+// chunk's counters are stashed on the device (a kernel, no copy engine) and
+// read once at the end: a blocking per-chunk read would queue behind the
+// large output copies and keep the host from issuing the next input copies,
+// serialising the two directions.
 bool exec_dense_pipelined(PlanImpl &P, int num, complex_t **in, complex_t **out, int chunk) {
   const size_t nb = sizeof(double) * 2 * (size_t)P.n;
   if (!ensure_slots(P, 2 * chunk)) return false;
   if (!P.in_stage.ensure(nb * 2 * chunk) || !P.dense_stage.ensure(nb * 2 * chunk) ||
-      !P.dense_ptrs.ensure(sizeof(void *) * 2 * chunk))
+      !P.dense_ptrs.ensure(sizeof(void *) * 2 * chunk) ||
+      !P.cnt_stash.ensure(sizeof(int) * sfft::CNT_STRIDE * (size_t)num))
     return false;
   cudaStream_t s = P.stream;
   const int nchunks = (num + chunk - 1) / chunk;
@@ -810,6 +820,10 @@ bool exec_dense_pipelined(PlanImpl &P, int num, complex_t **in, complex_t **out,
                                      (void *const *)P.dense_ptrs.p + base, m, s),
                  "scatter"))
       return false;
+    if (!cuda_ok(sfft::copy_ints(P.counters.as<int>() + (size_t)base * sfft::CNT_STRIDE,
+                                 P.cnt_stash.as<int>() + (size_t)i0 * sfft::CNT_STRIDE, sfft::CNT_STRIDE * m, s),
+                 "counter stash"))
+      return false;
     if (!cuda_ok(cudaEventRecord(P.ev_comp[half], s), "event")) return false;
     if (!cuda_ok(cudaStreamWaitEvent(P.copy_out, P.ev_comp[half], 0), "wait")) return false;
     for (int i = 0; i < m; i++)
@@ -817,15 +831,15 @@ bool exec_dense_pipelined(PlanImpl &P, int num, complex_t **in, complex_t **out,
                    "output copy"))
         return false;
     if (!cuda_ok(cudaEventRecord(P.ev_out[half], P.copy_out), "event")) return false;
-    if (c >= 1) {  // device errors of chunk c-1 once its transform is done
-      const int ph = (c - 1) & 1;
-      if (!cuda_ok(cudaEventSynchronize(P.ev_comp[ph]), "sync")) return false;
-      if (!check_device_errors(P, std::min(chunk, num - (c - 1) * chunk), ph * chunk)) return false;
+    if (c >= 1) {  // the host runs at most about one chunk ahead of the device
+      if (!cuda_ok(cudaEventSynchronize(P.ev_comp[(c - 1) & 1]), "sync")) return false;
     }
   }
   if (!cuda_ok(cudaStreamSynchronize(P.copy_out), "sync") || !cuda_ok(cudaStreamSynchronize(s), "sync")) return false;
-  const int last = nchunks - 1;
-  return check_device_errors(P, num - last * chunk, (last & 1) * chunk);
+  std::vector<int> cnt((size_t)sfft::CNT_STRIDE * num);
+  if (!cuda_ok(cudaMemcpy(cnt.data(), P.cnt_stash.p, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost), "counters"))
+    return false;
+  return check_counts(cnt.data(), num);
 }
 
 // sfft_exec_many with sparse results: like exec_dense_pipelined, chunk c's
@@ -1264,7 +1278,7 @@ long sfft_plan_footprint(const sfft_plan *plan) {
                         &P->score, &P->hits, &P->comb_bits, &P->comb_list, &P->counters, &P->out_idx,
                         &P->out_val, &P->man, &P->man_tmp, &P->g1, &P->g2, &P->perm, &P->est_f, &P->est_v, &P->map_keys,
                         &P->map_vals, &P->map_list, &P->rparams, &P->inputs, &P->dense_ptrs, &P->in_stage,
-                        &P->dense_stage, &P->trace};
+                        &P->dense_stage, &P->trace, &P->cnt_stash};
   long total = 0;
   for (const DBuf *b : bufs) total += (long)b->bytes;
   return total;

@@ -80,6 +80,9 @@ struct V12Dev {
 cudaError_t v12_run(const V12Dev &d, int nslots, cudaStream_t stream, StageEvents *se = nullptr);
 // Scatters the sparse result of each slot into dense n-point complex128
 // outputs (device array of per-slot pointers, already zeroed).
+// Device-to-device copy of `count` ints by a kernel (stream-ordered, no copy
+// engine involved).
+cudaError_t copy_ints(const int *src, int *dst, int count, cudaStream_t s);
 cudaError_t scatter_dense(const int *out_idx, const void *out_val, int prec, const int *counters,
                           int out_cap, void *const *dense, int nslots, cudaStream_t stream);
 

@@ -2006,6 +2006,18 @@ cudaError_t v12_run(const V12Dev &d, int nslots, cudaStream_t s, StageEvents *se
                               : run_typed<float, float2>(d, nslots, s, se);
 }
 
+__global__ void k_copy_ints(const int *src, int *dst, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = src[i];
+}
+
+cudaError_t copy_ints(const int *src, int *dst, int count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_copy_ints<<<(count + 255) / 256, 256, 0, s>>>(src, dst, count);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t scatter_dense(const int *out_idx, const void *out_val, int prec, const int *counters,
                           int out_cap, void *const *dense, int nslots, cudaStream_t s) {
   dim3 grid((out_cap + 255) / 256, nslots);
