@@ -243,6 +243,7 @@ __device__ void block_top_indices_f(KeyAt keyat, int N, int num, int *__restrict
           if (remaining >= acc && remaining < acc + c[q]) {
             hist[256] = lane * 8 + q;
             hist[257] = remaining - acc;
+            hist[258] = c[q];
           }
           acc += c[q];
         }
@@ -251,9 +252,30 @@ __device__ void block_top_indices_f(KeyAt keyat, int N, int num, int *__restrict
     __syncthreads();
     const int d = hist[256];
     remaining = hist[257];
+    const int in_bin = hist[258];
     prefix |= ((K)d) << shift;
     mask |= ((K)0xFF) << shift;
     __syncthreads();
+    if (in_bin == 1 && shift > 0) {
+      // the cutoff's bin holds a single key: that key is the cutoff, so its
+      // remaining digits need no further histogram passes
+      for (int i0 = 0; i0 < N; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        if (i < N) {
+          const K k = keyat(i);
+          if ((k & mask) == prefix) {
+            hist[260] = (int)(unsigned)(k & 0xffffffffu);
+            if constexpr (sizeof(K) == 8) hist[261] = (int)(unsigned)(k >> 32);
+          }
+        }
+      }
+      __syncthreads();
+      K kk = (K)(unsigned)hist[260];
+      if constexpr (sizeof(K) == 8) kk |= ((K)(unsigned)hist[261]) << 32;
+      prefix = kk;
+      __syncthreads();
+      break;
+    }
   }
   const K cutoff = prefix;
   // contiguous chunk per thread, in index order
