@@ -117,6 +117,7 @@ V3_CASES = [
     (1 << 18, 100, 2),
     (1 << 20, 200, 3),
     (1 << 24, 1000, 1),    # C2 shape
+    (1 << 20, 500, 4),     # comb width 4096
     (1 << 20, 1700, 5),    # comb width 16384: Mansour FFTs in global memory
 ]
 
