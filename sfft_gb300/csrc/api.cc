@@ -373,7 +373,9 @@ bool ensure_slots(PlanImpl &P, int want) {
     while (P.table_cap < 2 * P.map_cap) P.table_cap <<= 1;
     P.out_cap = P.map_cap;
     if (!P.perm.ensure(16 * 2 * (size_t)(p.w_g2 + 2) * S)) return false;
-    if (p.W_Man > sfft::v3_max_smem_fft() && !P.man_tmp.ensure(64 * (size_t)p.W_Man * S)) return false;
+    if ((p.W_Man > sfft::v3_max_smem_fft() || sfft::v3_man_split(p.W_Man)) &&
+        !P.man_tmp.ensure(64 * (size_t)p.W_Man * S))
+      return false;
     if (!P.man.ensure(32 * (size_t)p.W_Man * S) || !P.g1.ensure(32 * (size_t)p.B_g1 * S) ||
         !P.g2.ensure(32 * (size_t)p.B_g2 * S) || !P.est_f.ensure(sizeof(int) * P.est_cap * S) ||
         !P.est_v.ensure(16 * (size_t)P.est_cap * S) || !P.map_keys.ensure(sizeof(int) * P.table_cap * S) ||
@@ -610,7 +612,7 @@ void shift_view(PlanImpl &P, sfft::V12Dev &d, int base, bool own_out) {
 void shift_view(PlanImpl &P, sfft::V3Dev &d, int base, bool own_out) {
   if (!base) return;
   shift(d.man, 32 * (size_t)d.W, base);
-  if (d.large_man) shift(d.man_tmp, 64 * (size_t)d.W, base);
+  if (d.large_man || sfft::v3_man_split(d.W)) shift(d.man_tmp, 64 * (size_t)d.W, base);
   shift(d.g1, 32 * (size_t)d.B1, base);
   shift(d.g2, 32 * (size_t)d.B2, base);
   shift(d.perm, 16 * 2 * (size_t)(d.w2 + 2), base);

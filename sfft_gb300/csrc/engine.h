@@ -171,6 +171,10 @@ struct V3Dev {
 cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t stream, StageEvents *se = nullptr);
 // Largest FP64 FFT the v3 filter kernel runs in shared memory.
 int v3_max_smem_fft();
+// Whether a v3 plan's Mansour comb FFT of W points runs as eight W/8-point
+// FFTs over eight CTAs and a radix-8 combination (W from 4096 up to the
+// shared-memory limit) instead of in one CTA of the filter kernel.
+inline bool v3_man_split(int W) { return W >= 4096 && W <= v3_max_smem_fft(); }
 // Batched complex128 FFTs of length N in global memory (the same stages as
 // the shared-memory FFT): narr arrays per slot, arr_stride apart, slots
 // slot_stride apart; b is scratch of the same shape; result in a.

@@ -6,8 +6,8 @@
 //                 Gaussian fold (:215-297), each followed by its
 //                 shared-memory FFT.  The permuted samples of the second
 //                 fold take the phases of the reference's running product
-//                 (:66-87), formed in double-double from tables of its
-//                 factor's powers, one sample per thread.
+//                 (:66-87), formed from tables of its factor's powers, one
+//                 sample per thread.
 //   k_v3_peel     one thread-block cluster (8 CTAs) per signal runs
 //                 alternate_fft's estimate / peel rounds (:784-1088):
 //                 bucket estimation spread over the cluster, subtraction of
@@ -35,45 +35,9 @@ __device__ __forceinline__ double2 ld_x(const void *base, int in_type, long i) {
 
 // --------------------------------------------------------------- filters --
 
-// Double-double numbers (hi + lo, |lo| <= ulp(hi) / 2) with the error-free
-// transformations of Knuth (TwoSum) and of Dekker with a fused
-// multiply-add (TwoProduct): sums and products to about 2^-104 relative.
-struct DD {
-  double hi, lo;
-};
-struct CDD {
-  DD re, im;
-};
-
-__device__ __forceinline__ DD dd_quick(double a, double b) {  // |a| >= |b|
-  const double s = __dadd_rn(a, b);
-  return DD{s, __dsub_rn(b, __dsub_rn(s, a))};
-}
-
-__device__ __forceinline__ DD dd_add(DD x, DD y) {
-  const double s = __dadd_rn(x.hi, y.hi);
-  const double bb = __dsub_rn(s, x.hi);
-  const double e = __dadd_rn(__dsub_rn(x.hi, __dsub_rn(s, bb)), __dsub_rn(y.hi, bb));
-  return dd_quick(s, __dadd_rn(e, __dadd_rn(x.lo, y.lo)));
-}
-
-__device__ __forceinline__ DD dd_neg(DD x) { return DD{-x.hi, -x.lo}; }
-
-__device__ __forceinline__ DD dd_mul(DD x, DD y) {
-  const double p = __dmul_rn(x.hi, y.hi);
-  const double e = __fma_rn(x.hi, y.hi, -p);
-  return dd_quick(p, __fma_rn(x.hi, y.lo, __fma_rn(x.lo, y.hi, e)));
-}
-
-__device__ __forceinline__ CDD cdd(double re, double im) { return CDD{DD{re, 0.0}, DD{im, 0.0}}; }
-
-__device__ __forceinline__ CDD cdd_mul(CDD a, CDD b) {
-  return CDD{dd_add(dd_mul(a.re, b.re), dd_neg(dd_mul(a.im, b.im))), dd_add(dd_mul(a.re, b.im), dd_mul(a.im, b.re))};
-}
-
 // Split of the permuted Gaussian fold's phase products into tables:
 // LO = the power of two at or above sqrt(count) entries of step^lo and
-// ceil(count / LO) of shift_0 step^(LO hi), 32 bytes each, in the filter
+// ceil(count / LO) of shift_0 step^(LO hi), 16 bytes each, in the filter
 // kernel's shared memory.
 __host__ __device__ __forceinline__ int v3_phase_lo(int count) {
   int lo = 1;
@@ -81,13 +45,14 @@ __host__ __device__ __forceinline__ int v3_phase_lo(int count) {
   return lo;
 }
 
-// a^e, e >= 0, by binary powering.
-__device__ __forceinline__ CDD cdd_pow(CDD a, int e) {
-  CDD r = cdd(1.0, 0.0);
+// a^e, e >= 0, by binary powering in FP64: about 2 log2(e) rounded complex
+// products, a relative error of a few 1e-15.
+__device__ __forceinline__ double2 cpow64(double2 a, int e) {
+  double2 r = make_double2(1.0, 0.0);
   while (e) {
-    if (e & 1) r = cdd_mul(r, a);
+    if (e & 1) r = cmul<double>(r, a);
     e >>= 1;
-    if (e) a = cdd_mul(a, a);
+    if (e) a = cmul<double>(a, a);
   }
   return r;
 }
@@ -142,31 +107,24 @@ __global__ void __launch_bounds__(1024) k_v3_filters(V3Dev d, int role0) {
     // sin), but the product is not replayed serially: on GB300's FP64 pipe a
     // one-thread chain of rounded complex multiplications costs about 64
     // cycles per operation (2945 steps at n = 2^24, k = 1000: 0.58 ms).
-    // Every thread instead forms shift_i = shift_0 * step^i in double-double
-    // arithmetic from two tables -- step^lo for lo < LO and shift_0 *
-    // step^(LO hi) -- built by binary powering, and rounds it to FP64.  It
-    // differs from the serial chain by that chain's own accumulated rounding
-    // (about i * 2^-53 relative), which is far inside the 1e-10 value
+    // Every thread instead forms shift_i = (shift_0 step^(LO hi)) step^lo
+    // from two tables built by binary powering, one sample per thread.  Its
+    // relative error, a few 1e-15, is below the serial chain's own
+    // accumulated rounding (about i * 2^-53) and far inside the 1e-10 value
     // tolerance against the reference.
     double2 *P = (double2 *)d.perm + (long)slot * (d.w2 + 2) * 2 + (long)l * (d.w2 + 2);
     const int count = chunks * N + 1;
     const int LO = v3_phase_lo(count), HI = (count + LO - 1) / LO;
-    CDD *tab = (CDD *)smem_raw;  // [LO] step^lo, then [HI] shift_0 step^(LO hi)
+    double2 *tab = (double2 *)smem_raw;  // [LO] step^lo, then [HI] shift_0 step^(LO hi)
     {
       const double a0 = 2 * kPi * ig * bb / d.n, a1 = 2 * kPi * ai * bb / d.n;
-      const CDD sh0 = cdd(cos(a0), sin(a0)), st = cdd(cos(a1), sin(a1));
-      for (int e = threadIdx.x; e < LO + HI; e += blockDim.x) {
-        if (e < LO) {
-          tab[e] = cdd_pow(st, e);
-        } else {
-          tab[e] = cdd_mul(sh0, cdd_pow(cdd_pow(st, LO), e - LO));
-        }
-      }
+      const double2 sh0 = make_double2(cos(a0), sin(a0)), st = make_double2(cos(a1), sin(a1));
+      for (int e = threadIdx.x; e < LO + HI; e += blockDim.x)
+        tab[e] = e < LO ? cpow64(st, e) : cmul<double>(sh0, cpow64(cpow64(st, LO), e - LO));
     }
     __syncthreads();
     for (int i = l + threadIdx.x; i < count; i += blockDim.x) {
-      const CDD sh = cdd_mul(tab[LO + i / LO], tab[i % LO]);
-      const double2 shift = make_double2(__dadd_rn(sh.re.hi, sh.re.lo), __dadd_rn(sh.im.hi, sh.im.lo));
+      const double2 shift = cmul<double>(tab[LO + i / LO], tab[i % LO]);
       const long index = (long)(((unsigned long long)ig + (unsigned long long)i * (unsigned)ai) % (unsigned)d.n);
       P[i - l] = cmul<double>(ld_x(x, d.in_type, index), shift);
     }
@@ -206,6 +164,67 @@ __global__ void k_v3_man_interleave(V3Dev d) {
 }
 
 int v3_max_smem_fft() { return 8192; }
+
+// Mansour comb FFT of W points (4096 <= W <= 8192) as eight W/8-point FFTs:
+// the one-CTA FP64 FFT of 8192 points in the filter kernel takes about 280 k
+// cycles on GB300's narrow FP64 pipe, one SM's worth.  CTA r of a (signal,
+// shift) transforms the samples a[8m + r] (m < M = W/8) in shared memory,
+// multiplies entry m by w_W^(r m) and stores Y_r; k_v3_man_combine then
+// forms X[k + M q] = sum_r Y_r[k] w_8^(r q) (a radix-2 FFT of 8 points per
+// k).  The arithmetic differs from the one-CTA Stockham order only in
+// rounding (the v3 results are held to 1e-10 of the reference's).
+constexpr int V3_MAN_SPLIT = 8;
+
+__global__ void __launch_bounds__(256) k_v3_man_split(V3Dev d) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = d.W / V3_MAN_SPLIT;
+  double2 *buf = (double2 *)smem_raw;  // [M]
+  double2 *tws = buf + M;              // [M]: w_M^e = w_W^(8 e)
+  const int r = blockIdx.x, l = blockIdx.y, slot = blockIdx.z;
+  const int *rp = d.rparams + (long)slot * d.rp_stride;
+  const unsigned long long mask = (unsigned long long)d.n - 1;
+  const long sigma = d.n / d.W, o = rp[3] + l;
+  const double2 *tw = (const double2 *)d.tw_man;
+  const void *x = d.inputs[slot];
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    tws[m] = __ldg(tw + V3_MAN_SPLIT * m);
+    buf[m] = ld_x(x, d.in_type, (long)((unsigned long long)(o + (long)(V3_MAN_SPLIT * m + r) * sigma) & mask));
+  }
+  __syncthreads();
+  block_fft<double, 1>(buf, M, 31 - __clz(M), tws);
+  double2 *Y = (double2 *)d.man_tmp + (long)slot * 4 * d.W + (long)l * d.W + (long)r * M;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) Y[m] = cmul<double>(buf[m], __ldg(tw + r * m));
+}
+
+__global__ void __launch_bounds__(128) k_v3_man_combine(V3Dev d) {
+  const int M = d.W / V3_MAN_SPLIT;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, l = blockIdx.y, slot = blockIdx.z;
+  if (k >= M) return;
+  const double2 *Y = (const double2 *)d.man_tmp + (long)slot * 4 * d.W + (long)l * d.W;
+  const double2 *tw = (const double2 *)d.tw_man;
+  double2 v[V3_MAN_SPLIT];
+  constexpr int br[V3_MAN_SPLIT] = {0, 4, 2, 6, 1, 5, 3, 7};  // bit-reversed r
+#pragma unroll
+  for (int i = 0; i < V3_MAN_SPLIT; i++) v[i] = Y[(long)br[i] * M + k];
+#pragma unroll
+  for (int h = 1; h < V3_MAN_SPLIT; h *= 2) {
+#pragma unroll
+    for (int s0 = 0; s0 < V3_MAN_SPLIT; s0 += 2 * h) {
+#pragma unroll
+      for (int j = 0; j < h; j++) {
+        // w_8^(j 8 / (2 h)) = w_W^(M j 8 / (2 h))
+        const double2 t = j ? cmul<double>(v[s0 + j + h], __ldg(tw + (long)M * j * (V3_MAN_SPLIT / (2 * h))))
+                            : v[s0 + j + h];
+        const double2 u = v[s0 + j];
+        v[s0 + j] = cadd<double>(u, t);
+        v[s0 + j + h] = csub<double>(u, t);
+      }
+    }
+  }
+  double2 *man = (double2 *)d.man + (long)slot * 2 * d.W;
+#pragma unroll
+  for (int q = 0; q < V3_MAN_SPLIT; q++) man[2 * (k + M * q) + l] = v[q];
+}
 
 // ------------------------------------------------------------------ peel --
 
@@ -702,10 +721,20 @@ cudaError_t v3_run(const V3Dev &d, int nslots, cudaStream_t s, StageEvents *se) 
   if (T < 32) T = 32;
   const int per = (Nmax / 4 + T - 1) / T;
   const int count2 = (d.w2 / d.B2) * d.B2 + 1, lo2 = v3_phase_lo(count2);
-  const size_t sm = std::max((size_t)Nmax * sizeof(double2), sizeof(CDD) * (size_t)(lo2 + (count2 + lo2 - 1) / lo2));
+  const size_t sm = std::max((size_t)Nmax * sizeof(double2), sizeof(double2) * (size_t)(lo2 + (count2 + lo2 - 1) / lo2));
   mark(se, s);
   int role0 = 0;
-  if (d.large_man) {
+  if (!d.large_man && v3_man_split(d.W)) {
+    const int M = d.W / V3_MAN_SPLIT;
+    const size_t msm = 2 * sizeof(double2) * (size_t)M;
+    if ((e = set_smem(k_v3_man_split, msm))) return e;
+    k_v3_man_split<<<dim3(V3_MAN_SPLIT, 2, nslots), 256, msm, s>>>(d);
+    if ((e = cudaGetLastError())) return e;
+    k_v3_man_combine<<<dim3((M + 127) / 128, 2, nslots), 128, 0, s>>>(d);
+    if ((e = cudaGetLastError())) return e;
+    note_launches(2);
+    role0 = 2;
+  } else if (d.large_man) {
     const dim3 g((d.W + 255) / 256, 2, nslots);
     k_v3_man_gather<<<g, 256, 0, s>>>(d);
     if ((e = cudaGetLastError())) return e;
