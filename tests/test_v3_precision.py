@@ -14,7 +14,9 @@ relative errors of about 1e-7.  The Mansour decode
 The buckets of the first Gaussian filter and of the Mansour comb are formed
 here in numpy from the oracle's plan (filter taps, random offsets of one
 exec), once in FP64 and once with FP32 inputs, taps, products, sums and FFT,
-and decoded with the reference's tests in FP64."""
+and decoded with the reference's tests in FP64.  A third test bounds the
+difference between the permuted filter's phase factors as the reference
+forms them (a running product) and as the GPU does (power tables)."""
 import numpy as np
 import pytest
 
@@ -87,7 +89,7 @@ def test_fp32_gaussian_filter_mislocates_tones(setup):
     print(f"Gaussian filter, C2: FP64 locates {int(right64.sum())} tones in {int(ok64.sum())} decoded buckets; "
           f"FP32 loses {lost} of them, {moved} decoded frequencies differ")
     assert right64.sum() >= 40                 # the FP64 decode finds tones (55 at this seed)
-    assert lost >= 0.2 * right64.sum()         # FP32 loses a large share of them (20 of 55)
+    assert lost >= 0.2 * right64.sum()         # FP32 loses a large share of them (22 of 55)
     assert moved >= 0.1 * ok64.sum()           # and moves many decoded frequencies (85 of 296)
 
 
@@ -102,3 +104,42 @@ def test_fp32_mansour_comb_decodes_the_same(setup):
     assert int(np.sum(both & np.isin(f64, pos))) >= 800   # the comb locates most tones (881 of 1000)
     rel = np.abs(v64[both] - v32[both]) / np.abs(v64[both])
     assert float(np.max(rel)) < 1e-6
+
+
+def test_phase_power_tables_match_the_running_product(setup):
+    """The permuted Gaussian's phase factors: the reference forms shift_i by
+    the running product shift_{i+1} = shift_i * step (computefourier-3.0.cc:
+    66-87); the GPU forms (shift_0 step^(LO hi)) step^lo from two tables
+    built by binary powering (FP64, separately rounded complex products).
+    At the C2 shape both stay within 1e-12 of each other (the chain's own
+    rounding drift), far inside the 1e-10 value tolerance."""
+    _, _, _, op, p, dbg = setup
+    ig, ai, b = dbg["init_G_offset"], dbg["ai"], dbg["b"]
+    count = (p["w_g2"] // p["B_g2"]) * p["B_g2"] + 1
+    a0, a1 = 2 * np.pi * ig * b / N, 2 * np.pi * ai * b / N   # the reference's angles
+    sh0, st = complex(np.cos(a0), np.sin(a0)), complex(np.cos(a1), np.sin(a1))
+    chain = np.empty(count, dtype=np.complex128)
+    sh = sh0
+    for i in range(count):
+        chain[i] = sh
+        sh = sh * st
+
+    def cpow(a, e):
+        r = 1 + 0j
+        while e:
+            if e & 1:
+                r = r * a
+            e >>= 1
+            if e:
+                a = a * a
+        return r
+
+    lo = 1
+    while lo * lo < count:
+        lo *= 2
+    hi = (count + lo - 1) // lo
+    t_lo = [cpow(st, e) for e in range(lo)]
+    s_lo = cpow(st, lo)
+    t_hi = [sh0 * cpow(s_lo, h) for h in range(hi)]
+    tab = np.array([t_hi[i // lo] * t_lo[i % lo] for i in range(count)])
+    assert float(np.max(np.abs(tab - chain))) < 1e-12
