@@ -1330,8 +1330,8 @@ void sfft_exec_many(sfft_plan *plan, int num, complex_t **in, complex_t **out) {
   bool all_host = num > 1;
   for (int i = 0; i < num && all_host; i++)
     if (is_device_ptr(in[i]) || is_device_ptr(out[i])) all_host = false;
-  if (all_host) {  // about 16 chunks: copies overlap the transforms with little fill and drain
-    exec_dense_pipelined(*P, num, in, out, std::max(1, std::min(chunk, (num + 15) / 16)));
+  if (all_host) {  // about 32 chunks: copies overlap the transforms with little fill and drain
+    exec_dense_pipelined(*P, num, in, out, std::max(1, std::min(chunk, (num + 31) / 32)));
     return;
   }
   if (!ensure_slots(*P, chunk)) return;
@@ -1404,7 +1404,7 @@ int sfft_exec_many_sparse(sfft_plan *plan, int num, const complex_t *const *in, 
   std::lock_guard<std::mutex> g(P->mu);
   cudaSetDevice(P->device);
   g_err.clear();
-  const int chunk = std::max(1, std::min(P->max_batch, (num + 15) / 16));  // about 16 pipelined chunks
+  const int chunk = std::max(1, std::min(P->max_batch, (num + 31) / 32));  // about 32 pipelined chunks
   return exec_sparse_pipelined(*P, num, in, out_idx, out_val, out_count, out_stride, chunk) ? 0 : -1;
 }
 
