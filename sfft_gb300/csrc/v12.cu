@@ -1476,6 +1476,7 @@ static cudaError_t launch_comb(const V12Dev &d, int nslots, cudaStream_t s) {
       return cudaErrorInvalidValue;
   }
 #undef SFFT_COMB
+  note_launches(1);
   return cudaGetLastError();
 }
 
